@@ -1,0 +1,85 @@
+// Host-side launchers of the CUDA kernels (implemented in kernels.cu and
+// bottom.cu).  Every launcher enqueues on `stream` and returns the launch's
+// cudaError_t; none of them synchronises.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "agb_types.h"
+
+namespace agb {
+
+template <typename T>
+LevelGeom<T> make_geom(int nx, int ny, int nz, const double dx[3]);
+
+// f = A u (Operator::Elastic::Fapply)
+template <typename T>
+cudaError_t launch_fapply(int sym, const T* u, const T* C, const LevelGeom<T>& G, const BcTable& bc, T* f,
+                          cudaStream_t s);
+// diag of A (Operator::Elastic::Diagonal)
+template <typename T>
+cudaError_t launch_diagonal(int sym, const T* C, const LevelGeom<T>& G, const BcTable& bc, T* diag, cudaStream_t s);
+// One damped-Jacobi sweep fused with the operator:
+//   xout = (1-w) x + w (b - (A x - diag x)) / diag     (x == nullptr: x = 0)
+template <typename T>
+cudaError_t launch_jacobi(int sym, const T* x, const T* b, const T* diag, const T* C, const LevelGeom<T>& G,
+                          const BcTable& bc, T omega, T* xout, cudaStream_t s);
+// r = b - A x; when `partials` is non-null each block also writes its
+// max |r| and sum r^2 (as doubles) to partials[2*block], partials[2*block+1]
+template <typename T>
+cudaError_t launch_residual(int sym, const T* x, const T* b, const T* C, const LevelGeom<T>& G, const BcTable& bc,
+                            T* r, double* partials, int* nblocks_out, cudaStream_t s);
+// block count the residual kernel uses for a level (sizes the partials buffer)
+int residual_blocks(int nx, int ny, int nz);
+// norms[0] = max over blocks, norms[1] = sqrt(sum) over blocks
+cudaError_t launch_reduce_norms(const double* partials, int nblocks, double* norms, cudaStream_t s);
+// max |v| and sum v^2 of a plain vector, same partials convention
+cudaError_t launch_vec_norms(const double* v, int64_t n, double* partials, int nblocks, double* norms,
+                             cudaStream_t s);
+
+// nodal full weighting of a 3-component field, fine level -> coarse level
+template <typename T>
+cudaError_t launch_restrict(const T* fine, const LevelGeom<T>& Gf, T* crse, const LevelGeom<T>& Gc, cudaStream_t s);
+// same weights on nc stiffness components (SoA)
+cudaError_t launch_restrict_C(const double* Cf, const LevelGeom<double>& Gf, double* Cc, const LevelGeom<double>& Gc,
+                              int nc, cudaStream_t s);
+// fine += P crse (trilinear nodal prolongation)
+template <typename T>
+cudaError_t launch_prolong_add(const T* crse, const LevelGeom<T>& Gc, T* fine, const LevelGeom<T>& Gf,
+                               cudaStream_t s);
+
+// layout and precision helpers
+cudaError_t launch_aos_to_soa(const double* aos, double* soa, int64_t N, int nc, cudaStream_t s);
+cudaError_t launch_soa_to_aos(const double* soa, double* aos, int64_t N, int nc, cudaStream_t s);
+cudaError_t launch_to_float(const double* in, float* out, int64_t n, double scale, cudaStream_t s);
+// out(double) += scale * in(float)
+cudaError_t launch_add_float(const float* in, double* out, int64_t n, double scale, cudaStream_t s);
+cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStream_t s);
+
+// BC::Operator::Elastic::Constant::Init: boundary values into b
+cudaError_t launch_bc_init(double* b, const LevelGeom<double>& G, const BcTable& bc, const double* bcval_dev,
+                           int homogeneous, cudaStream_t s);
+// Newton RHS (src/Solver/Nonlocal/Newton.H:144-231): dw = C (grad u - F0),
+// rhs = b - div dw (interior) or b - BC(u, grad u, dw) (boundary)
+cudaError_t launch_build_rhs(int sym, const double* u, const double* b, const double* F0, int f0_ncomp,
+                             const double* C, const LevelGeom<double>& G, const BcTable& bc, double* dw, double* rhs,
+                             cudaStream_t s);
+// stress = C (grad u - F0), strain = sym grad u (9 values per node, AoS
+// row-major), energy = 0.5 sigma:eps; any output may be null
+cudaError_t launch_stress_strain(int sym, const double* u, const double* F0, int f0_ncomp, const double* C,
+                                 const LevelGeom<double>& G, double* stress, double* strain, double* energy,
+                                 cudaStream_t s);
+
+// Bottom solve on the coarsest level in one thread block: BiCGStab on the
+// diagonally normalised system (the reference's normalize), FP64, followed by
+// `nsmooth_ok` Fsmooth calls after success or, after a breakdown, a zeroed
+// correction and `nsmooth_fail` calls.  work: 7 * 3N doubles;
+// info[0] = BiCGStab return code, info[1] = iterations.
+cudaError_t launch_bottom_bicgstab_ex(int sym, const double* C, const double* diag, const LevelGeom<double>& G,
+                                      const BcTable& bc, const double* rhs, double* sol, double* work, int max_iter,
+                                      double tol_rel, double tol_abs, int nsmooth_ok, int nsmooth_fail, double omega,
+                                      int* info, cudaStream_t s);
+cudaError_t launch_bottom_bicgstab(int sym, const double* C, const double* diag, const LevelGeom<double>& G,
+                                   const BcTable& bc, const double* rhs, double* sol, double* work, int max_iter,
+                                   double tol_rel, double tol_abs, int* info, cudaStream_t s);
+
+}  // namespace agb

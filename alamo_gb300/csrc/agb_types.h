@@ -1,0 +1,45 @@
+// Plain data types shared by the host driver (compiled by g++) and the CUDA
+// kernels (compiled by nvcc).
+#pragma once
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define AGB_HD __host__ __device__
+#else
+#define AGB_HD
+#endif
+
+namespace agb {
+
+enum { SYM_ISO = 0, SYM_MM = 1 };
+enum { BC_DISP = 0, BC_TRAC = 1, BC_PERIODIC = 2, BC_NEUMANN = 3, BC_NONE = 4 };
+
+// Boundary-condition types: region * 3 + component, region order of the
+// reference's Face enum (src/BC/Operator/Elastic/Elastic.H:35-43).
+struct BcTable {
+    unsigned char t[78];
+};
+
+// One multigrid level's geometry and the scaling constants derived from dx.
+template <typename T>
+struct LevelGeom {
+    int nx, ny, nz;
+    int64_t N;       // nodes
+    int64_t sy, sz;  // strides of j and k
+    T h[3];          // 0.5 / dx  (central first derivative)
+    T inv[3];        // 1 / dx    (one-sided first derivative)
+    T i2[3];         // 1 / dx^2  (second derivative)
+    T q[3];          // 0.25 / (dx_a dx_b) for the pairs xy, xz, yz
+};
+
+// index of the 21 major-minor entries by Voigt-pair (00,01,02,11,12,22) rows
+// and columns: upper triangle of the symmetric 6x6 matrix, row-major
+// (src/Set/Matrix4_MajorMinor.H:327-375)
+AGB_HD constexpr int mm_ut(int a, int b) {
+    return a <= b ? (a * 11 - a * a) / 2 + b : (b * 11 - b * b) / 2 + a;
+}
+AGB_HD constexpr int pair_of(int i, int j) {
+    return (i == j) ? (i == 0 ? 0 : i == 1 ? 3 : 5) : ((i + j) == 1 ? 1 : (i + j) == 2 ? 2 : 4);
+}
+
+}  // namespace agb

@@ -1,0 +1,989 @@
+// Host driver of alamo_gb300: the C ABI of include/agb.h, the multigrid
+// hierarchy, the V-cycle and the solves.
+//
+// Mapping to the reference (Gopal-B/alamo):
+//   agb_elastic            Operator::Elastic<SYM> + Solver::Nonlocal::Linear
+//                          (one AMR level, every multigrid level on one GPU)
+//   prepare()              Operator<Grid::Node>::prepareForSolve
+//                          (src/Operator/Operator.cpp:253-260)
+//   vcycle<T>()            the MLMG V-cycle that calls the operator's hooks
+//                          (Fsmooth, correctionResidual, restriction,
+//                          interpolation, bottom BiCGStab)
+//   solve_fp64 / mixed     Linear::solve (src/Solver/Nonlocal/Linear.H:131)
+//   agb_newton_solve       Newton::solve, nriters = 1
+//                          (src/Solver/Nonlocal/Newton.H:279-358)
+// Nothing here falls back to the CPU: every array operation is a CUDA kernel.
+#include "../../include/agb.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "agb_launch.h"
+
+using namespace agb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+agb_status fail(agb_status st, const std::string& msg) {
+    g_last_error = msg;
+    return st;
+}
+
+#define CK(call)                                                                                         \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess) {                                                                         \
+            return fail(e_ == cudaErrorMemoryAllocation ? AGB_OUT_OF_MEMORY : AGB_CUDA_ERROR,            \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                             \
+        }                                                                                                \
+    } while (0)
+
+#define TRY(call)                        \
+    do {                                 \
+        agb_status s_ = (call);          \
+        if (s_ != AGB_OK) return s_;     \
+    } while (0)
+
+template <typename T>
+struct Lev {
+    LevelGeom<T> G;
+    T* C = nullptr;       // SoA stiffness (nc * N)
+    T* diag = nullptr;    // 3N
+    T* res = nullptr;     // right-hand side of the level's correction equation
+    T* cor = nullptr;     // correction
+    T* rescor = nullptr;  // res - A cor
+    T* tmp = nullptr;     // Jacobi ping-pong buffer
+};
+
+}  // namespace
+
+struct agb_elastic {
+    int sym = 0, nc = 2;
+    int n[3] = {0, 0, 0};
+    double dx[3] = {1, 1, 1};
+    agb_solver_opts opts{};
+    BcTable bc{};
+    double bcval[78] = {0};
+    bool model_set = false, bc_set = true, prepared = false, have_f32 = false;
+    int device = 0;
+    std::vector<Lev<double>> L64;
+    std::vector<Lev<float>> L32;
+    std::vector<double> ldx;  // cell sizes per level (3 each)
+    cudaStream_t stream = nullptr, own_stream = nullptr;
+    double* partials = nullptr;
+    int partials_cap = 0;
+    double* norms_dev = nullptr;
+    double* norms_host = nullptr;  // pinned
+    double* bottom_work = nullptr;
+    int* bottom_info = nullptr;
+    double* bcval_dev = nullptr;
+    // staging buffers for host-pointer calls and scratch (allocated on demand)
+    double* io[4] = {nullptr, nullptr, nullptr, nullptr};
+    size_t io_cap[4] = {0, 0, 0, 0};
+    double* dw = nullptr;  // 9N scratch of the Newton RHS
+    // profiling
+    bool prof = false;
+    int64_t prof_count[AGB_K_NFAMILIES] = {0};
+    double prof_ms[AGB_K_NFAMILIES] = {0};
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+    size_t ev_used = 0;
+    int64_t launches = 0;
+};
+
+namespace {
+
+int64_t nodes(const agb_elastic* h) { return (int64_t)h->n[0] * h->n[1] * h->n[2]; }
+
+agb_status ensure_io(agb_elastic* h, int slot, size_t bytes) {
+    if (h->io_cap[slot] >= bytes) return AGB_OK;
+    if (h->io[slot]) cudaFree(h->io[slot]);
+    h->io[slot] = nullptr;
+    h->io_cap[slot] = 0;
+    CK(cudaMalloc(&h->io[slot], bytes));
+    h->io_cap[slot] = bytes;
+    return AGB_OK;
+}
+
+// ---------------------------------------------------------------- profiling
+struct ProfScope {
+    agb_elastic* h;
+    int fam;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(agb_elastic* hh, int f, bool on) : h(hh), fam(f) {
+        if (!on || !h->prof) { h = nullptr; return; }
+        if (h->ev_used + 2 > h->ev_pool.size()) {
+            for (int q = 0; q < 64; q++) {
+                cudaEvent_t e;
+                cudaEventCreate(&e);
+                h->ev_pool.push_back(e);
+            }
+        }
+        a = h->ev_pool[h->ev_used++];
+        b = h->ev_pool[h->ev_used++];
+        cudaEventRecord(a, h->stream);
+    }
+    ~ProfScope() {
+        if (!h) return;
+        cudaEventRecord(b, h->stream);
+        h->ev_pending.push_back({fam, {a, b}});
+    }
+};
+
+void prof_collect(agb_elastic* h) {
+    if (h->ev_pending.empty()) return;
+    cudaStreamSynchronize(h->stream);
+    for (auto& p : h->ev_pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) {
+            h->prof_count[p.first] += 1;
+            h->prof_ms[p.first] += ms;
+        }
+    }
+    h->ev_pending.clear();
+    h->ev_used = 0;
+}
+
+// ---------------------------------------------------------------- buffers
+template <typename T>
+void free_levels(std::vector<Lev<T>>& L) {
+    for (auto& l : L) {
+        cudaFree(l.C); cudaFree(l.diag); cudaFree(l.res); cudaFree(l.cor); cudaFree(l.rescor); cudaFree(l.tmp);
+    }
+    L.clear();
+}
+
+int num_levels(const int n0[3], int max_coarsening_level) {
+    int n[3] = {n0[0], n0[1], n0[2]};
+    int lev = 1;
+    while (max_coarsening_level < 0 || lev - 1 < max_coarsening_level) {
+        bool ok = true;
+        for (int d = 0; d < 3; d++) {
+            const int cells = n[d] - 1;
+            if (cells % 2 != 0 || cells / 2 < 2) ok = false;
+        }
+        if (!ok) break;
+        for (int d = 0; d < 3; d++) n[d] = (n[d] - 1) / 2 + 1;
+        lev++;
+    }
+    return lev;
+}
+
+agb_status alloc_levels64(agb_elastic* h) {
+    free_levels(h->L64);
+    const int nl = num_levels(h->n, h->opts.max_coarsening_level);
+    h->ldx.assign(3 * nl, 0.0);
+    int n[3] = {h->n[0], h->n[1], h->n[2]};
+    double dx[3] = {h->dx[0], h->dx[1], h->dx[2]};
+    h->L64.resize(nl);
+    int maxblocks = 0;
+    for (int l = 0; l < nl; l++) {
+        Lev<double>& v = h->L64[l];
+        v.G = make_geom<double>(n[0], n[1], n[2], dx);
+        for (int d = 0; d < 3; d++) h->ldx[3 * l + d] = dx[d];
+        const size_t N = (size_t)v.G.N;
+        CK(cudaMalloc(&v.C, sizeof(double) * N * h->nc));
+        CK(cudaMalloc(&v.diag, sizeof(double) * 3 * N));
+        CK(cudaMalloc(&v.res, sizeof(double) * 3 * N));
+        CK(cudaMalloc(&v.cor, sizeof(double) * 3 * N));
+        CK(cudaMalloc(&v.rescor, sizeof(double) * 3 * N));
+        CK(cudaMalloc(&v.tmp, sizeof(double) * 3 * N));
+        maxblocks = std::max(maxblocks, residual_blocks(n[0], n[1], n[2]));
+        for (int d = 0; d < 3; d++) { n[d] = (n[d] - 1) / 2 + 1; dx[d] *= 2; }
+    }
+    maxblocks = std::max(maxblocks, 152 * 16);
+    if (h->partials_cap < maxblocks) {
+        cudaFree(h->partials);
+        h->partials = nullptr;
+        CK(cudaMalloc(&h->partials, sizeof(double) * 2 * maxblocks));
+        h->partials_cap = maxblocks;
+    }
+    const Lev<double>& b = h->L64.back();
+    cudaFree(h->bottom_work);
+    h->bottom_work = nullptr;
+    CK(cudaMalloc(&h->bottom_work, sizeof(double) * 7 * 3 * (size_t)b.G.N));
+    return AGB_OK;
+}
+
+agb_status alloc_levels32(agb_elastic* h) {
+    free_levels(h->L32);
+    const int nl = (int)h->L64.size();
+    h->L32.resize(nl);
+    for (int l = 0; l < nl; l++) {
+        Lev<float>& v = h->L32[l];
+        v.G = make_geom<float>(h->L64[l].G.nx, h->L64[l].G.ny, h->L64[l].G.nz, &h->ldx[3 * l]);
+        const size_t N = (size_t)v.G.N;
+        CK(cudaMalloc(&v.C, sizeof(float) * N * h->nc));
+        CK(cudaMalloc(&v.diag, sizeof(float) * 3 * N));
+        CK(cudaMalloc(&v.res, sizeof(float) * 3 * N));
+        CK(cudaMalloc(&v.cor, sizeof(float) * 3 * N));
+        CK(cudaMalloc(&v.rescor, sizeof(float) * 3 * N));
+        CK(cudaMalloc(&v.tmp, sizeof(float) * 3 * N));
+    }
+    return AGB_OK;
+}
+
+// ---------------------------------------------------------------- prepare
+agb_status prepare(agb_elastic* h) {
+    if (h->prepared) return AGB_OK;
+    if (!h->model_set) return fail(AGB_NOT_READY, "model not set (agb_elastic_set_model)");
+    const int nl = (int)h->L64.size();
+    for (int l = 1; l < nl; l++) {
+        CK(launch_restrict_C(h->L64[l - 1].C, h->L64[l - 1].G, h->L64[l].C, h->L64[l].G, h->nc, h->stream));
+        h->launches++;
+    }
+    for (int l = 0; l < nl; l++) {
+        CK(launch_diagonal<double>(h->sym, h->L64[l].C, h->L64[l].G, h->bc, h->L64[l].diag, h->stream));
+        h->launches++;
+    }
+    if (h->opts.precision == AGB_PRECISION_MIXED) {
+        if (h->L32.size() != h->L64.size()) TRY(alloc_levels32(h));
+        for (int l = 0; l < nl; l++) {
+            CK(launch_to_float(h->L64[l].C, h->L32[l].C, h->L64[l].G.N * h->nc, 1.0, h->stream));
+            CK(launch_diagonal<float>(h->sym, h->L32[l].C, h->L32[l].G, h->bc, h->L32[l].diag, h->stream));
+            h->launches += 2;
+        }
+        h->have_f32 = true;
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    h->prepared = true;
+    return AGB_OK;
+}
+
+agb_status ensure_f32(agb_elastic* h) {
+    TRY(prepare(h));
+    if (h->have_f32) return AGB_OK;
+    const int nl = (int)h->L64.size();
+    if (h->L32.size() != h->L64.size()) TRY(alloc_levels32(h));
+    for (int l = 0; l < nl; l++) {
+        CK(launch_to_float(h->L64[l].C, h->L32[l].C, h->L64[l].G.N * h->nc, 1.0, h->stream));
+        CK(launch_diagonal<float>(h->sym, h->L32[l].C, h->L32[l].G, h->bc, h->L32[l].diag, h->stream));
+        h->launches += 2;
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    h->have_f32 = true;
+    return AGB_OK;
+}
+
+// ---------------------------------------------------------------- cycle
+template <typename T>
+struct Fam;
+template <>
+struct Fam<double> { enum { J = AGB_K_JACOBI_F64, R = AGB_K_RESIDUAL_F64 }; };
+template <>
+struct Fam<float> { enum { J = AGB_K_JACOBI_F32, R = AGB_K_RESIDUAL_F32 }; };
+
+// ncalls Fsmooth calls (2 sweeps each) on level l; cor_zero: cor is known 0
+template <typename T>
+agb_status smooth(agb_elastic* h, std::vector<Lev<T>>& L, int l, int ncalls, bool cor_zero) {
+    Lev<T>& v = L[l];
+    const T w = (T)h->opts.omega;
+    const int sweeps = 2 * ncalls;
+    if (sweeps == 0 && cor_zero) {
+        CK(cudaMemsetAsync(v.cor, 0, sizeof(T) * 3 * v.G.N, h->stream));
+        return AGB_OK;
+    }
+    for (int s = 0; s < sweeps; s++) {
+        {
+            ProfScope ps(h, Fam<T>::J, l == 0 && !(cor_zero && s == 0));
+            CK(launch_jacobi<T>(h->sym, (cor_zero && s == 0) ? nullptr : v.cor, v.res, v.diag, v.C, v.G, h->bc, w,
+                                v.tmp, h->stream));
+        }
+        h->launches++;
+        std::swap(v.cor, v.tmp);
+    }
+    return AGB_OK;
+}
+
+agb_status bottom64(agb_elastic* h, Lev<double>& b) {
+    CK(cudaMemsetAsync(b.cor, 0, sizeof(double) * 3 * b.G.N, h->stream));
+    ProfScope ps(h, AGB_K_BOTTOM, true);
+    CK(launch_bottom_bicgstab_ex(h->sym, b.C, b.diag, b.G, h->bc, b.res, b.cor, h->bottom_work,
+                                 h->opts.bottom_max_iter, h->opts.bottom_tol_rel, h->opts.bottom_tol_abs,
+                                 h->opts.bottom_smooth, h->opts.final_smooth, h->opts.omega, h->bottom_info,
+                                 h->stream));
+    h->launches++;
+    return AGB_OK;
+}
+
+template <typename T>
+agb_status bottom(agb_elastic* h, std::vector<Lev<T>>& L);
+template <>
+agb_status bottom<double>(agb_elastic* h, std::vector<Lev<double>>& L) {
+    return bottom64(h, L.back());
+}
+template <>
+agb_status bottom<float>(agb_elastic* h, std::vector<Lev<float>>& L) {
+    // the bottom solve stays FP64: widen the coarse residual, solve, narrow
+    Lev<float>& f = L.back();
+    Lev<double>& d = h->L64.back();
+    const int64_t n3 = 3 * f.G.N;
+    CK(cudaMemsetAsync(d.res, 0, sizeof(double) * n3, h->stream));
+    CK(launch_add_float(f.res, d.res, n3, 1.0, h->stream));
+    TRY(bottom64(h, d));
+    CK(launch_to_float(d.cor, f.cor, n3, 1.0, h->stream));
+    h->launches += 2;
+    return AGB_OK;
+}
+
+// One V-cycle on the correction equation A cor = res of level 0
+// (MLMG::mgVcycle as driven by the reference's hooks).
+template <typename T>
+agb_status vcycle(agb_elastic* h, std::vector<Lev<T>>& L) {
+    const int nl = (int)L.size();
+    for (int l = 0; l < nl - 1; l++) {
+        Lev<T>& v = L[l];
+        TRY(smooth<T>(h, L, l, h->opts.pre_smooth, true));
+        {
+            ProfScope ps(h, Fam<T>::R, l == 0);
+            CK(launch_residual<T>(h->sym, v.cor, v.res, v.C, v.G, h->bc, v.rescor, nullptr, nullptr, h->stream));
+        }
+        {
+            ProfScope ps(h, AGB_K_RESTRICT, l == 0);
+            CK(launch_restrict<T>(v.rescor, v.G, L[l + 1].res, L[l + 1].G, h->stream));
+        }
+        h->launches += 2;
+    }
+    TRY(bottom<T>(h, L));
+    for (int l = nl - 2; l >= 0; l--) {
+        {
+            ProfScope ps(h, AGB_K_PROLONG, l == 0);
+            CK(launch_prolong_add<T>(L[l + 1].cor, L[l + 1].G, L[l].cor, L[l].G, h->stream));
+        }
+        h->launches++;
+        TRY(smooth<T>(h, L, l, h->opts.post_smooth, false));
+    }
+    return AGB_OK;
+}
+
+// FP64 residual of level 0 into L64[0].res and its norms (host copy)
+agb_status residual64(agb_elastic* h, const double* x, const double* rhs, double out[2]) {
+    Lev<double>& v = h->L64[0];
+    int nb = 0;
+    {
+        ProfScope ps(h, AGB_K_RESIDUAL_F64, true);
+        CK(launch_residual<double>(h->sym, x, rhs, v.C, v.G, h->bc, v.res, h->partials, &nb, h->stream));
+    }
+    CK(launch_reduce_norms(h->partials, nb, h->norms_dev, h->stream));
+    h->launches += 2;
+    CK(cudaMemcpyAsync(h->norms_host, h->norms_dev, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    out[0] = h->norms_host[0];
+    out[1] = h->norms_host[1];
+    return AGB_OK;
+}
+
+agb_status vec_norms(agb_elastic* h, const double* v, int64_t n, double out[2]) {
+    CK(launch_vec_norms(v, n, h->partials, std::min(h->partials_cap, 152 * 8), h->norms_dev, h->stream));
+    h->launches += 2;
+    CK(cudaMemcpyAsync(h->norms_host, h->norms_dev, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    out[0] = h->norms_host[0];
+    out[1] = h->norms_host[1];
+    return AGB_OK;
+}
+
+// Linear::solve on device pointers.
+agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_rel, double tol_abs,
+                     agb_solve_report* rep) {
+    auto t0 = std::chrono::steady_clock::now();
+    TRY(prepare(h));
+    const bool mixed = h->opts.precision == AGB_PRECISION_MIXED;
+    if (mixed) TRY(ensure_f32(h));
+    Lev<double>& top = h->L64[0];
+    const int64_t n3 = 3 * top.G.N;
+    double r[2], bn[2];
+    TRY(residual64(h, x, rhs, r));
+    TRY(vec_norms(h, rhs, n3, bn));
+    int fp64_res = 1;
+    const double resnorm0 = r[0];
+    const double max_norm = (bn[0] >= resnorm0) ? bn[0] : resnorm0;
+    const double target = std::max(tol_abs, std::max(tol_rel, 1.e-16) * max_norm);
+    const bool fixed = h->opts.fixed_iter > 0;
+    const int maxit = fixed ? h->opts.fixed_iter : h->opts.max_iter;
+    int status = AGB_NOT_CONVERGED, it = 0;
+    if (std::isnan(r[0]) || std::isnan(r[1])) status = AGB_NAN;
+    else if (r[0] <= target && !fixed) status = AGB_OK;
+    else {
+        while (it < maxit) {
+            if (!mixed) {
+                TRY(vcycle<double>(h, h->L64));
+                CK(launch_axpy(1.0, top.cor, x, n3, h->stream));
+                h->launches++;
+                it++;
+            } else {
+                // FP32 cycles on the scaled FP64 residual, FP64 update
+                const double s = (r[0] > 0.0) ? 1.0 / r[0] : 1.0;
+                Lev<float>& t32 = h->L32[0];
+                CK(launch_to_float(top.res, t32.res, n3, s, h->stream));
+                h->launches++;
+                const int inner = std::max(1, h->opts.inner_cycles);
+                for (int c = 0; c < inner && it < maxit; c++) {
+                    TRY(vcycle<float>(h, h->L32));
+                    CK(launch_add_float(t32.cor, x, n3, 1.0 / s, h->stream));
+                    h->launches++;
+                    it++;
+                    if (c + 1 < inner && it < maxit) {
+                        // next FP32 cycle works on res - A cor of the scaled correction equation
+                        ProfScope ps(h, AGB_K_RESIDUAL_F32, true);
+                        CK(launch_residual<float>(h->sym, t32.cor, t32.res, t32.C, t32.G, h->bc, t32.rescor, nullptr,
+                                                  nullptr, h->stream));
+                        h->launches++;
+                        std::swap(t32.res, t32.rescor);
+                    }
+                }
+            }
+            TRY(residual64(h, x, rhs, r));
+            fp64_res++;
+            if (h->opts.verbose > 0) std::fprintf(stderr, "agb: cycle %d |r|_inf = %.6e\n", it, r[0]);
+            if (std::isnan(r[0]) || std::isnan(r[1])) { status = AGB_NAN; break; }
+            if (r[0] <= target && !fixed) { status = AGB_OK; break; }
+        }
+        if (fixed && status != AGB_NAN) status = AGB_OK;
+    }
+    int binfo[2] = {0, 0};
+    CK(cudaMemcpyAsync(h->norms_host, h->bottom_info, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    std::memcpy(binfo, h->norms_host, 2 * sizeof(int));
+    prof_collect(h);
+    if (rep) {
+        rep->status = status;
+        rep->iters = it;
+        rep->nlevels = (int)h->L64.size();
+        rep->bottom_iters = binfo[1];
+        rep->fp64_residuals = fp64_res;
+        rep->resnorm0 = resnorm0;
+        rep->rhsnorm0 = bn[0];
+        rep->final_resnorm = r[0];
+        rep->final_resnorm_l2 = r[1];
+        rep->rhsnorm_l2 = bn[1];
+        rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    if (status == AGB_NOT_CONVERGED) g_last_error = "multigrid did not reach the tolerance within max_iter cycles";
+    if (status == AGB_NAN) g_last_error = "NaN in the residual";
+    return (agb_status)status;
+}
+
+// copy a host or device input of `bytes` into a device pointer
+agb_status dev_in(agb_elastic* h, int slot, const void* src, size_t bytes, int where, const void** out) {
+    if (where == AGB_MEM_DEVICE) { *out = src; return AGB_OK; }
+    if (where != AGB_MEM_HOST) return fail(AGB_BAD_ARG, "where must be AGB_MEM_HOST or AGB_MEM_DEVICE");
+    TRY(ensure_io(h, slot, bytes));
+    CK(cudaMemcpyAsync(h->io[slot], src, bytes, cudaMemcpyHostToDevice, h->stream));
+    *out = h->io[slot];
+    return AGB_OK;
+}
+// device pointer an output lands in before it is copied back to `dst`
+agb_status dev_out(agb_elastic* h, int slot, void* dst, size_t bytes, int where, void** out) {
+    if (where == AGB_MEM_DEVICE) { *out = dst; return AGB_OK; }
+    if (where != AGB_MEM_HOST) return fail(AGB_BAD_ARG, "where must be AGB_MEM_HOST or AGB_MEM_DEVICE");
+    TRY(ensure_io(h, slot, bytes));
+    *out = h->io[slot];
+    return AGB_OK;
+}
+agb_status finish_out(agb_elastic* h, void* dst, const void* dev, size_t bytes, int where) {
+    if (where == AGB_MEM_HOST) CK(cudaMemcpyAsync(dst, dev, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return AGB_OK;
+}
+
+agb_status check_level(agb_elastic* h, int level) {
+    if (!h) return fail(AGB_BAD_ARG, "null handle");
+    if (level < 0 || level >= (int)h->L64.size()) return fail(AGB_BAD_ARG, "level out of range");
+    if (level > 0 || !h->model_set) TRY(prepare(h));
+    return AGB_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+agb_status agb_default_opts(agb_solver_opts* o) {
+    if (!o) return fail(AGB_BAD_ARG, "null opts");
+    o->max_iter = 200;
+    o->pre_smooth = 2;
+    o->post_smooth = 2;
+    o->final_smooth = 8;
+    o->bottom_smooth = 0;
+    o->bottom_max_iter = 200;
+    o->bottom_tol_rel = 1e-4;
+    o->bottom_tol_abs = -1.0;
+    o->omega = 2.0 / 3.0;
+    o->max_coarsening_level = -1;
+    o->fixed_iter = -1;
+    o->verbose = 0;
+    o->precision = AGB_PRECISION_FP64;
+    o->inner_cycles = 1;
+    return AGB_OK;
+}
+
+static agb_status check_opts(const agb_solver_opts* o) {
+    if (o->pre_smooth < 0 || o->post_smooth < 0 || o->final_smooth < 0 || o->bottom_smooth < 0 ||
+        o->bottom_max_iter < 0 || o->max_iter < 0)
+        return fail(AGB_BAD_ARG, "negative iteration count in opts");
+    if (!(o->omega > 0.0) || !(o->omega <= 2.0)) return fail(AGB_BAD_ARG, "omega must lie in (0, 2]");
+    if (o->precision != AGB_PRECISION_FP64 && o->precision != AGB_PRECISION_MIXED)
+        return fail(AGB_BAD_ARG, "unknown precision");
+    return AGB_OK;
+}
+
+agb_status agb_elastic_create(agb_elastic** out, int nx, int ny, int nz, const double dx[3], int sym,
+                              const agb_solver_opts* opts) {
+    if (!out) return fail(AGB_BAD_ARG, "null output handle");
+    *out = nullptr;
+    if (nx < 3 || ny < 3 || nz < 3) return fail(AGB_BAD_ARG, "grid needs at least 3 nodes per axis");
+    if (!dx || !(dx[0] > 0) || !(dx[1] > 0) || !(dx[2] > 0)) return fail(AGB_BAD_ARG, "dx must be positive");
+    if (sym != AGB_SYM_ISOTROPIC && sym != AGB_SYM_MAJORMINOR) return fail(AGB_BAD_ARG, "unknown symmetry");
+    agb_elastic* h = new agb_elastic();
+    h->sym = sym;
+    h->nc = sym == AGB_SYM_ISOTROPIC ? 2 : 21;
+    h->n[0] = nx; h->n[1] = ny; h->n[2] = nz;
+    for (int d = 0; d < 3; d++) h->dx[d] = dx[d];
+    if (opts) {
+        agb_status st = check_opts(opts);
+        if (st != AGB_OK) { delete h; return st; }
+        h->opts = *opts;
+    } else {
+        agb_default_opts(&h->opts);
+    }
+    // default BC: displacement 0 everywhere (Constant.H:36-45)
+    for (int q = 0; q < 78; q++) { h->bc.t[q] = BC_DISP; h->bcval[q] = 0.0; }
+    auto bail = [&](agb_status st) { agb_elastic_destroy(h); return st; };
+    if (cudaGetDevice(&h->device) != cudaSuccess) return bail(fail(AGB_CUDA_ERROR, "no CUDA device"));
+    if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(AGB_CUDA_ERROR, "cudaStreamCreate failed"));
+    h->stream = h->own_stream;
+    agb_status st = alloc_levels64(h);
+    if (st != AGB_OK) return bail(st);
+    if (cudaMalloc(&h->norms_dev, 4 * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost(&h->norms_host, 4 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&h->bottom_info, 4 * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&h->bcval_dev, 78 * sizeof(double)) != cudaSuccess)
+        return bail(fail(AGB_OUT_OF_MEMORY, "allocation of small buffers failed"));
+    cudaMemset(h->bottom_info, 0, 4 * sizeof(int));
+    *out = h;
+    return AGB_OK;
+}
+
+agb_status agb_elastic_destroy(agb_elastic* h) {
+    if (!h) return AGB_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_levels(h->L64);
+    free_levels(h->L32);
+    cudaFree(h->partials);
+    cudaFree(h->norms_dev);
+    if (h->norms_host) cudaFreeHost(h->norms_host);
+    cudaFree(h->bottom_work);
+    cudaFree(h->bottom_info);
+    cudaFree(h->bcval_dev);
+    cudaFree(h->dw);
+    for (int s = 0; s < 4; s++) cudaFree(h->io[s]);
+    for (auto e : h->ev_pool) cudaEventDestroy(e);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    delete h;
+    return AGB_OK;
+}
+
+agb_status agb_elastic_set_opts(agb_elastic* h, const agb_solver_opts* o) {
+    if (!h || !o) return fail(AGB_BAD_ARG, "null argument");
+    TRY(check_opts(o));
+    const bool relevel = o->max_coarsening_level != h->opts.max_coarsening_level;
+    h->opts = *o;
+    if (relevel) {
+        // keep the fine-level stiffness across the re-allocation
+        const int64_t N = nodes(h);
+        double* keep = nullptr;
+        if (h->model_set) {
+            CK(cudaMalloc(&keep, sizeof(double) * N * h->nc));
+            CK(cudaMemcpyAsync(keep, h->L64[0].C, sizeof(double) * N * h->nc, cudaMemcpyDeviceToDevice, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+        }
+        free_levels(h->L32);
+        h->have_f32 = false;
+        agb_status st = alloc_levels64(h);
+        if (st == AGB_OK && keep)
+            st = (cudaMemcpy(h->L64[0].C, keep, sizeof(double) * N * h->nc, cudaMemcpyDeviceToDevice) == cudaSuccess)
+                     ? AGB_OK
+                     : fail(AGB_CUDA_ERROR, "copy of the stiffness failed");
+        cudaFree(keep);
+        if (st != AGB_OK) return st;
+    }
+    h->prepared = false;
+    h->have_f32 = false;
+    return AGB_OK;
+}
+
+agb_status agb_elastic_set_stream(agb_elastic* h, void* s) {
+    if (!h) return fail(AGB_BAD_ARG, "null handle");
+    CK(cudaStreamSynchronize(h->stream));
+    h->stream = s ? (cudaStream_t)s : h->own_stream;
+    return AGB_OK;
+}
+
+agb_status agb_elastic_set_model(agb_elastic* h, const double* C, int where) {
+    if (!h || !C) return fail(AGB_BAD_ARG, "null argument");
+    const int64_t N = nodes(h);
+    const size_t bytes = sizeof(double) * N * h->nc;
+    const void* src = nullptr;
+    if (where == AGB_MEM_HOST) {
+        // stage through a stream-ordered temporary, then AoS -> SoA
+        double* tmp = nullptr;
+        CK(cudaMallocAsync((void**)&tmp, bytes, h->stream));
+        CK(cudaMemcpyAsync(tmp, C, bytes, cudaMemcpyHostToDevice, h->stream));
+        CK(launch_aos_to_soa(tmp, h->L64[0].C, N, h->nc, h->stream));
+        CK(cudaFreeAsync(tmp, h->stream));
+    } else if (where == AGB_MEM_DEVICE) {
+        src = C;
+        CK(launch_aos_to_soa((const double*)src, h->L64[0].C, N, h->nc, h->stream));
+    } else {
+        return fail(AGB_BAD_ARG, "where must be AGB_MEM_HOST or AGB_MEM_DEVICE");
+    }
+    h->launches++;
+    CK(cudaStreamSynchronize(h->stream));
+    h->model_set = true;
+    h->prepared = false;
+    h->have_f32 = false;
+    return AGB_OK;
+}
+
+agb_status agb_elastic_get_model(agb_elastic* h, int level, double* C, int where) {
+    TRY(check_level(h, level));
+    if (!C) return fail(AGB_BAD_ARG, "null output");
+    Lev<double>& v = h->L64[level];
+    const size_t bytes = sizeof(double) * v.G.N * h->nc;
+    void* d = nullptr;
+    TRY(dev_out(h, 0, C, bytes, where, &d));
+    CK(launch_soa_to_aos(v.C, (double*)d, v.G.N, h->nc, h->stream));
+    h->launches++;
+    return finish_out(h, C, d, bytes, where);
+}
+
+agb_status agb_elastic_set_bc(agb_elastic* h, const int* type, const double* val) {
+    if (!h || !type || !val) return fail(AGB_BAD_ARG, "null argument");
+    for (int q = 0; q < 78; q++) {
+        if (type[q] < AGB_BC_DISPLACEMENT || type[q] > AGB_BC_NONE) return fail(AGB_BAD_ARG, "unknown BC type");
+    }
+    for (int q = 0; q < 78; q++) { h->bc.t[q] = (unsigned char)type[q]; h->bcval[q] = val[q]; }
+    h->bc_set = true;
+    h->prepared = false;
+    h->have_f32 = false;
+    return AGB_OK;
+}
+
+agb_status agb_elastic_prepare(agb_elastic* h) {
+    if (!h) return fail(AGB_BAD_ARG, "null handle");
+    return prepare(h);
+}
+
+agb_status agb_elastic_num_levels(agb_elastic* h, int* nl) {
+    if (!h || !nl) return fail(AGB_BAD_ARG, "null argument");
+    *nl = (int)h->L64.size();
+    return AGB_OK;
+}
+
+agb_status agb_elastic_level_dims(agb_elastic* h, int level, int dims[3]) {
+    if (!h || !dims) return fail(AGB_BAD_ARG, "null argument");
+    if (level < 0 || level >= (int)h->L64.size()) return fail(AGB_BAD_ARG, "level out of range");
+    dims[0] = h->L64[level].G.nx; dims[1] = h->L64[level].G.ny; dims[2] = h->L64[level].G.nz;
+    return AGB_OK;
+}
+
+agb_status agb_elastic_fapply(agb_elastic* h, int level, const double* u, double* f, int where) {
+    TRY(check_level(h, level));
+    if (!u || !f) return fail(AGB_BAD_ARG, "null argument");
+    Lev<double>& v = h->L64[level];
+    const size_t bytes = sizeof(double) * 3 * v.G.N;
+    const void* du = nullptr;
+    void* df = nullptr;
+    TRY(dev_in(h, 0, u, bytes, where, &du));
+    TRY(dev_out(h, 1, f, bytes, where, &df));
+    {
+        ProfScope ps(h, AGB_K_FAPPLY_F64, level == 0);
+        CK(launch_fapply<double>(h->sym, (const double*)du, v.C, v.G, h->bc, (double*)df, h->stream));
+    }
+    h->launches++;
+    TRY(finish_out(h, f, df, bytes, where));
+    prof_collect(h);
+    return AGB_OK;
+}
+
+agb_status agb_elastic_fapply_f32(agb_elastic* h, int level, const float* u, float* f, int where) {
+    TRY(check_level(h, level));
+    if (!u || !f) return fail(AGB_BAD_ARG, "null argument");
+    TRY(ensure_f32(h));
+    Lev<float>& v = h->L32[level];
+    const size_t bytes = sizeof(float) * 3 * v.G.N;
+    const void* du = nullptr;
+    void* df = nullptr;
+    TRY(dev_in(h, 0, u, bytes, where, &du));
+    TRY(dev_out(h, 1, f, bytes, where, &df));
+    {
+        ProfScope ps(h, AGB_K_FAPPLY_F32, level == 0);
+        CK(launch_fapply<float>(h->sym, (const float*)du, v.C, v.G, h->bc, (float*)df, h->stream));
+    }
+    h->launches++;
+    TRY(finish_out(h, f, df, bytes, where));
+    prof_collect(h);
+    return AGB_OK;
+}
+
+agb_status agb_elastic_diagonal(agb_elastic* h, int level, double* diag, int where) {
+    TRY(check_level(h, level));
+    TRY(prepare(h));
+    if (!diag) return fail(AGB_BAD_ARG, "null argument");
+    Lev<double>& v = h->L64[level];
+    const size_t bytes = sizeof(double) * 3 * v.G.N;
+    if (where == AGB_MEM_HOST) CK(cudaMemcpyAsync(diag, v.diag, bytes, cudaMemcpyDeviceToHost, h->stream));
+    else CK(cudaMemcpyAsync(diag, v.diag, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return AGB_OK;
+}
+
+agb_status agb_elastic_fsmooth(agb_elastic* h, int level, double* x, const double* b, int ncalls, int where) {
+    TRY(check_level(h, level));
+    TRY(prepare(h));
+    if (!x || !b || ncalls < 0) return fail(AGB_BAD_ARG, "bad argument");
+    Lev<double>& v = h->L64[level];
+    const size_t bytes = sizeof(double) * 3 * v.G.N;
+    const void* dx0 = nullptr;
+    const void* db = nullptr;
+    TRY(dev_in(h, 0, x, bytes, where, &dx0));
+    TRY(dev_in(h, 1, b, bytes, where, &db));
+    // the level's cor/res buffers hold the iterate and the rhs
+    CK(cudaMemcpyAsync(v.cor, dx0, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(v.res, db, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    TRY(smooth<double>(h, h->L64, level, ncalls, false));
+    if (where == AGB_MEM_HOST) CK(cudaMemcpyAsync(x, v.cor, bytes, cudaMemcpyDeviceToHost, h->stream));
+    else CK(cudaMemcpyAsync(x, v.cor, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    prof_collect(h);
+    return AGB_OK;
+}
+
+agb_status agb_elastic_residual(agb_elastic* h, int level, const double* x, const double* b, double* r,
+                                double norms[2], int where) {
+    TRY(check_level(h, level));
+    if (!x || !b || !r) return fail(AGB_BAD_ARG, "null argument");
+    Lev<double>& v = h->L64[level];
+    const size_t bytes = sizeof(double) * 3 * v.G.N;
+    const void* dx0 = nullptr;
+    const void* db = nullptr;
+    void* dr = nullptr;
+    TRY(dev_in(h, 0, x, bytes, where, &dx0));
+    TRY(dev_in(h, 1, b, bytes, where, &db));
+    TRY(dev_out(h, 2, r, bytes, where, &dr));
+    int nb = 0;
+    {
+        ProfScope ps(h, AGB_K_RESIDUAL_F64, level == 0);
+        CK(launch_residual<double>(h->sym, (const double*)dx0, (const double*)db, v.C, v.G, h->bc, (double*)dr,
+                                   h->partials, &nb, h->stream));
+    }
+    CK(launch_reduce_norms(h->partials, nb, h->norms_dev, h->stream));
+    h->launches += 2;
+    CK(cudaMemcpyAsync(h->norms_host, h->norms_dev, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TRY(finish_out(h, r, dr, bytes, where));
+    if (norms) { norms[0] = h->norms_host[0]; norms[1] = h->norms_host[1]; }
+    prof_collect(h);
+    return AGB_OK;
+}
+
+agb_status agb_elastic_restrict(agb_elastic* h, int crse_level, const double* fine, double* crse, int where) {
+    if (!h) return fail(AGB_BAD_ARG, "null handle");
+    if (crse_level < 1 || crse_level >= (int)h->L64.size()) return fail(AGB_BAD_ARG, "level out of range");
+    if (!fine || !crse) return fail(AGB_BAD_ARG, "null argument");
+    Lev<double>& f = h->L64[crse_level - 1];
+    Lev<double>& c = h->L64[crse_level];
+    const void* df = nullptr;
+    void* dc = nullptr;
+    TRY(dev_in(h, 0, fine, sizeof(double) * 3 * f.G.N, where, &df));
+    TRY(dev_out(h, 1, crse, sizeof(double) * 3 * c.G.N, where, &dc));
+    CK(launch_restrict<double>((const double*)df, f.G, (double*)dc, c.G, h->stream));
+    h->launches++;
+    return finish_out(h, crse, dc, sizeof(double) * 3 * c.G.N, where);
+}
+
+agb_status agb_elastic_prolong_add(agb_elastic* h, int fine_level, const double* crse, double* fine, int where) {
+    if (!h) return fail(AGB_BAD_ARG, "null handle");
+    if (fine_level < 0 || fine_level + 1 >= (int)h->L64.size()) return fail(AGB_BAD_ARG, "level out of range");
+    if (!fine || !crse) return fail(AGB_BAD_ARG, "null argument");
+    Lev<double>& f = h->L64[fine_level];
+    Lev<double>& c = h->L64[fine_level + 1];
+    const size_t fb = sizeof(double) * 3 * f.G.N;
+    const void* dc = nullptr;
+    const void* df0 = nullptr;
+    TRY(dev_in(h, 0, crse, sizeof(double) * 3 * c.G.N, where, &dc));
+    TRY(dev_in(h, 1, fine, fb, where, &df0));
+    CK(launch_prolong_add<double>((const double*)dc, c.G, (double*)df0, f.G, h->stream));
+    h->launches++;
+    return finish_out(h, fine, df0, fb, where);
+}
+
+agb_status agb_elastic_bc_init(agb_elastic* h, double* b, int homogeneous, int where) {
+    if (!h || !b) return fail(AGB_BAD_ARG, "null argument");
+    const size_t bytes = sizeof(double) * 3 * nodes(h);
+    const void* db = nullptr;
+    TRY(dev_in(h, 0, b, bytes, where, &db));
+    CK(cudaMemcpyAsync(h->bcval_dev, h->bcval, sizeof(h->bcval), cudaMemcpyHostToDevice, h->stream));
+    CK(launch_bc_init((double*)db, h->L64[0].G, h->bc, h->bcval_dev, homogeneous, h->stream));
+    h->launches++;
+    return finish_out(h, b, db, bytes, where);
+}
+
+static agb_status build_rhs_dev(agb_elastic* h, const double* u, const double* b, const double* F0, int f0n,
+                                double* rhs) {
+    const int64_t N = nodes(h);
+    if (!h->dw) CK(cudaMalloc(&h->dw, sizeof(double) * 9 * N));
+    CK(launch_build_rhs(h->sym, u, b, F0, f0n, h->L64[0].C, h->L64[0].G, h->bc, h->dw, rhs, h->stream));
+    h->launches += 2;
+    return AGB_OK;
+}
+
+agb_status agb_elastic_build_rhs(agb_elastic* h, const double* u, const double* b, const double* F0, int f0_ncomp,
+                                 double* rhs, int where) {
+    if (!h || !u || !b || !rhs) return fail(AGB_BAD_ARG, "null argument");
+    if (!(f0_ncomp == 0 || f0_ncomp == 1 || f0_ncomp == 9) || (f0_ncomp && !F0))
+        return fail(AGB_BAD_ARG, "f0_ncomp must be 0, 1 or 9 (with F0 given)");
+    if (!h->model_set) return fail(AGB_NOT_READY, "model not set");
+    const int64_t N = nodes(h);
+    const size_t bytes = sizeof(double) * 3 * N;
+    const void *du = nullptr, *db = nullptr, *dF = nullptr;
+    void* dr = nullptr;
+    TRY(dev_in(h, 0, u, bytes, where, &du));
+    TRY(dev_in(h, 1, b, bytes, where, &db));
+    if (f0_ncomp) TRY(dev_in(h, 3, F0, sizeof(double) * f0_ncomp * N, where, &dF));
+    TRY(dev_out(h, 2, rhs, bytes, where, &dr));
+    TRY(build_rhs_dev(h, (const double*)du, (const double*)db, (const double*)dF, f0_ncomp, (double*)dr));
+    return finish_out(h, rhs, dr, bytes, where);
+}
+
+agb_status agb_linear_solve(agb_elastic* h, double* sol, const double* rhs, double tol_rel, double tol_abs,
+                            agb_solve_report* rep, int where) {
+    if (!h || !sol || !rhs) return fail(AGB_BAD_ARG, "null argument");
+    const size_t bytes = sizeof(double) * 3 * nodes(h);
+    const void *dx0 = nullptr, *dr = nullptr;
+    TRY(dev_in(h, 0, sol, bytes, where, &dx0));
+    TRY(dev_in(h, 1, rhs, bytes, where, &dr));
+    agb_status st = solve_dev(h, (double*)dx0, (const double*)dr, tol_rel, tol_abs, rep);
+    if (st == AGB_OK || st == AGB_NOT_CONVERGED || st == AGB_NAN) {
+        agb_status s2 = finish_out(h, sol, dx0, bytes, where);
+        if (s2 != AGB_OK) return s2;
+    }
+    return st;
+}
+
+agb_status agb_newton_solve(agb_elastic* h, double* u, const double* b, const double* F0, int f0_ncomp,
+                            double tol_rel, double tol_abs, agb_solve_report* rep, int where) {
+    if (!h || !u || !b) return fail(AGB_BAD_ARG, "null argument");
+    if (!(f0_ncomp == 0 || f0_ncomp == 1 || f0_ncomp == 9) || (f0_ncomp && !F0))
+        return fail(AGB_BAD_ARG, "f0_ncomp must be 0, 1 or 9 (with F0 given)");
+    if (!h->model_set) return fail(AGB_NOT_READY, "model not set");
+    auto t0 = std::chrono::steady_clock::now();
+    const int64_t N = nodes(h);
+    const size_t bytes = sizeof(double) * 3 * N;
+    const void *du = nullptr, *db = nullptr, *dF = nullptr;
+    TRY(dev_in(h, 0, u, bytes, where, &du));
+    TRY(dev_in(h, 1, b, bytes, where, &db));
+    if (f0_ncomp) TRY(dev_in(h, 3, F0, sizeof(double) * f0_ncomp * N, where, &dF));
+    TRY(ensure_io(h, 2, 2 * bytes));
+    double* rhs = h->io[2];
+    double* du_inc = h->io[2] + 3 * N;
+    TRY(build_rhs_dev(h, (const double*)du, (const double*)db, (const double*)dF, f0_ncomp, rhs));
+    CK(cudaMemsetAsync(du_inc, 0, bytes, h->stream));
+    agb_status st = solve_dev(h, du_inc, rhs, tol_rel, tol_abs, rep);
+    if (st != AGB_OK && st != AGB_NOT_CONVERGED) return st;
+    CK(launch_axpy(1.0, du_inc, (double*)du, 3 * N, h->stream));
+    h->launches++;
+    agb_status s2 = finish_out(h, u, du, bytes, where);
+    if (s2 != AGB_OK) return s2;
+    if (rep) rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return st;
+}
+
+agb_status agb_elastic_stress_strain(agb_elastic* h, const double* u, const double* F0, int f0_ncomp, double* stress,
+                                     double* strain, double* energy, int where) {
+    if (!h || !u) return fail(AGB_BAD_ARG, "null argument");
+    if (!(f0_ncomp == 0 || f0_ncomp == 1 || f0_ncomp == 9) || (f0_ncomp && !F0))
+        return fail(AGB_BAD_ARG, "f0_ncomp must be 0, 1 or 9 (with F0 given)");
+    if (!h->model_set) return fail(AGB_NOT_READY, "model not set");
+    const int64_t N = nodes(h);
+    const void *du = nullptr, *dF = nullptr;
+    TRY(dev_in(h, 0, u, sizeof(double) * 3 * N, where, &du));
+    if (f0_ncomp) TRY(dev_in(h, 3, F0, sizeof(double) * f0_ncomp * N, where, &dF));
+    double *ds = nullptr, *de = nullptr, *den = nullptr;
+    if (where == AGB_MEM_DEVICE) {
+        ds = stress; de = strain; den = energy;
+    } else {
+        if (!h->dw) CK(cudaMalloc(&h->dw, sizeof(double) * 9 * N));
+        TRY(ensure_io(h, 1, sizeof(double) * 10 * N));
+        ds = stress ? h->dw : nullptr;
+        de = strain ? h->io[1] : nullptr;
+        den = energy ? h->io[1] + 9 * N : nullptr;
+    }
+    CK(launch_stress_strain(h->sym, (const double*)du, (const double*)dF, f0_ncomp, h->L64[0].C, h->L64[0].G, ds, de,
+                            den, h->stream));
+    h->launches++;
+    if (where == AGB_MEM_HOST) {
+        if (stress) CK(cudaMemcpyAsync(stress, ds, sizeof(double) * 9 * N, cudaMemcpyDeviceToHost, h->stream));
+        if (strain) CK(cudaMemcpyAsync(strain, de, sizeof(double) * 9 * N, cudaMemcpyDeviceToHost, h->stream));
+        if (energy) CK(cudaMemcpyAsync(energy, den, sizeof(double) * N, cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    return AGB_OK;
+}
+
+agb_status agb_profile_enable(agb_elastic* h, int on) {
+    if (!h) return fail(AGB_BAD_ARG, "null handle");
+    h->prof = on != 0;
+    return AGB_OK;
+}
+
+agb_status agb_profile_reset(agb_elastic* h) {
+    if (!h) return fail(AGB_BAD_ARG, "null handle");
+    prof_collect(h);
+    for (int f = 0; f < AGB_K_NFAMILIES; f++) { h->prof_count[f] = 0; h->prof_ms[f] = 0.0; }
+    return AGB_OK;
+}
+
+agb_status agb_profile_get(agb_elastic* h, int family, int64_t* launches, double* ms) {
+    if (!h || family < 0 || family >= AGB_K_NFAMILIES) return fail(AGB_BAD_ARG, "bad argument");
+    prof_collect(h);
+    if (launches) *launches = h->prof_count[family];
+    if (ms) *ms = h->prof_ms[family];
+    return AGB_OK;
+}
+
+agb_status agb_launch_count(agb_elastic* h, int64_t* n) {
+    if (!h || !n) return fail(AGB_BAD_ARG, "null argument");
+    *n = h->launches;
+    return AGB_OK;
+}
+
+const char* agb_status_string(int s) {
+    switch (s) {
+        case AGB_OK: return "AGB_OK";
+        case AGB_NOT_CONVERGED: return "AGB_NOT_CONVERGED";
+        case AGB_NAN: return "AGB_NAN";
+        case AGB_BAD_ARG: return "AGB_BAD_ARG";
+        case AGB_CUDA_ERROR: return "AGB_CUDA_ERROR";
+        case AGB_NOT_READY: return "AGB_NOT_READY";
+        case AGB_OUT_OF_MEMORY: return "AGB_OUT_OF_MEMORY";
+        case AGB_LIMIT: return "AGB_LIMIT";
+        default: return "AGB_UNKNOWN";
+    }
+}
+
+const char* agb_last_error(void) { return g_last_error.c_str(); }
+
+const char* agb_version(void) { return "alamo_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

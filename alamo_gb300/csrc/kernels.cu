@@ -1,0 +1,566 @@
+// Field kernels of the nodal elastic multigrid path, sm_103a.
+//
+// All node fields are SoA per component with x fastest and no ghost nodes;
+// boundary nodes of the domain carry the boundary-condition rows, so every
+// stencil stays inside the grid.  One thread owns one node; blocks are
+// 32 x 4 x 2 nodes so a warp reads 32 consecutive x-nodes (coalesced
+// 256-byte rows in FP64) and the y/z neighbours of a block hit L1/L2.
+#include <cuda_runtime.h>
+#include <cmath>
+#include "agb_launch.h"
+#include "operator.cuh"
+
+namespace agb {
+
+static constexpr int BX = 32, BY = 4, BZ = 2;
+
+static inline dim3 grid3(int nx, int ny, int nz) { return dim3((nx + BX - 1) / BX, (ny + BY - 1) / BY, (nz + BZ - 1) / BZ); }
+
+template <typename T>
+LevelGeom<T> make_geom(int nx, int ny, int nz, const double dx[3]) {
+    LevelGeom<T> G;
+    G.nx = nx; G.ny = ny; G.nz = nz;
+    G.sy = nx;
+    G.sz = (int64_t)nx * ny;
+    G.N = G.sz * nz;
+    for (int d = 0; d < 3; d++) {
+        G.h[d] = T(0.5 / dx[d]);
+        G.inv[d] = T(1.0 / dx[d]);
+        G.i2[d] = T(1.0 / (dx[d] * dx[d]));
+    }
+    G.q[0] = T(0.25 / (dx[0] * dx[1]));
+    G.q[1] = T(0.25 / (dx[0] * dx[2]));
+    G.q[2] = T(0.25 / (dx[1] * dx[2]));
+    return G;
+}
+template LevelGeom<double> make_geom<double>(int, int, int, const double*);
+template LevelGeom<float> make_geom<float>(int, int, int, const double*);
+
+#define AGB_NODE_INDEX                                    \
+    const int i = blockIdx.x * BX + threadIdx.x;          \
+    const int j = blockIdx.y * BY + threadIdx.y;          \
+    const int k = blockIdx.z * BZ + threadIdx.z;          \
+    const bool live = (i < G.nx) & (j < G.ny) & (k < G.nz); \
+    const int64_t id = i + G.sy * j + G.sz * k;
+
+// ---------------------------------------------------------------- Fapply
+template <typename T, int SYM>
+__global__ void __launch_bounds__(256) k_fapply(const T* __restrict__ u, const T* __restrict__ C, LevelGeom<T> G,
+                                                BcTable bc, T* __restrict__ f) {
+    AGB_NODE_INDEX
+    if (!live) return;
+    T r[3];
+    apply_node<T, SYM>(u, C, G, bc, i, j, k, id, r);
+    f[id] = r[0];
+    f[G.N + id] = r[1];
+    f[2 * G.N + id] = r[2];
+}
+
+template <typename T>
+cudaError_t launch_fapply(int sym, const T* u, const T* C, const LevelGeom<T>& G, const BcTable& bc, T* f,
+                          cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
+    if (sym == SYM_ISO) k_fapply<T, SYM_ISO><<<grd, blk, 0, s>>>(u, C, G, bc, f);
+    else k_fapply<T, SYM_MM><<<grd, blk, 0, s>>>(u, C, G, bc, f);
+    return cudaGetLastError();
+}
+template cudaError_t launch_fapply<double>(int, const double*, const double*, const LevelGeom<double>&, const BcTable&,
+                                           double*, cudaStream_t);
+template cudaError_t launch_fapply<float>(int, const float*, const float*, const LevelGeom<float>&, const BcTable&,
+                                          float*, cudaStream_t);
+
+// ---------------------------------------------------------------- Diagonal
+template <typename T, int SYM>
+__global__ void __launch_bounds__(256) k_diag(const T* __restrict__ C, LevelGeom<T> G, BcTable bc, T* __restrict__ dg) {
+    AGB_NODE_INDEX
+    if (!live) return;
+    T r[3];
+    diag_node<T, SYM>(C, G, bc, i, j, k, id, r);
+    dg[id] = r[0];
+    dg[G.N + id] = r[1];
+    dg[2 * G.N + id] = r[2];
+}
+
+template <typename T>
+cudaError_t launch_diagonal(int sym, const T* C, const LevelGeom<T>& G, const BcTable& bc, T* diag, cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
+    if (sym == SYM_ISO) k_diag<T, SYM_ISO><<<grd, blk, 0, s>>>(C, G, bc, diag);
+    else k_diag<T, SYM_MM><<<grd, blk, 0, s>>>(C, G, bc, diag);
+    return cudaGetLastError();
+}
+template cudaError_t launch_diagonal<double>(int, const double*, const LevelGeom<double>&, const BcTable&, double*,
+                                             cudaStream_t);
+template cudaError_t launch_diagonal<float>(int, const float*, const LevelGeom<float>&, const BcTable&, float*,
+                                            cudaStream_t);
+
+// ---------------------------------------------------------------- Jacobi
+// One damped-Jacobi sweep of Operator<Grid::Node>::Fsmooth
+// (src/Operator/Operator.cpp:109-146) fused with the operator application:
+// Ax is never written to memory.
+template <typename T, int SYM>
+__global__ void __launch_bounds__(256) k_jacobi(const T* __restrict__ x, const T* __restrict__ b,
+                                                const T* __restrict__ dg, const T* __restrict__ C, LevelGeom<T> G,
+                                                BcTable bc, T omega, T* __restrict__ xo) {
+    AGB_NODE_INDEX
+    if (!live) return;
+    T ax[3];
+    apply_node<T, SYM>(x, C, G, bc, i, j, k, id, ax);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const int64_t q = c * G.N + id;
+        const T xv = x[q], d = dg[q];
+        const T rx = ax[c] - xv * d;
+        xo[q] = (T(1) - omega) * xv + omega * (b[q] - rx) / d;
+    }
+}
+
+// first sweep from a zero guess: A 0 = 0, so x = w b / diag
+template <typename T>
+__global__ void k_jacobi_zero(const T* __restrict__ b, const T* __restrict__ dg, T omega, T* __restrict__ xo,
+                              int64_t n) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        xo[q] = omega * (b[q] - T(0)) / dg[q];
+}
+
+static inline int flat_blocks(int64_t n) {
+    int64_t b = (n + 255) / 256;
+    return (int)(b < 152 * 16 ? (b < 1 ? 1 : b) : 152 * 16);
+}
+
+template <typename T>
+cudaError_t launch_jacobi(int sym, const T* x, const T* b, const T* diag, const T* C, const LevelGeom<T>& G,
+                          const BcTable& bc, T omega, T* xout, cudaStream_t s) {
+    if (x == nullptr) {
+        const int64_t n = 3 * G.N;
+        k_jacobi_zero<T><<<flat_blocks(n), 256, 0, s>>>(b, diag, omega, xout, n);
+        return cudaGetLastError();
+    }
+    dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
+    if (sym == SYM_ISO) k_jacobi<T, SYM_ISO><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
+    else k_jacobi<T, SYM_MM><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
+    return cudaGetLastError();
+}
+template cudaError_t launch_jacobi<double>(int, const double*, const double*, const double*, const double*,
+                                           const LevelGeom<double>&, const BcTable&, double, double*, cudaStream_t);
+template cudaError_t launch_jacobi<float>(int, const float*, const float*, const float*, const float*,
+                                          const LevelGeom<float>&, const BcTable&, float, float*, cudaStream_t);
+
+// ---------------------------------------------------------------- residual
+// Block reduction of (max, sum) pairs: warp shuffles, then one warp over the
+// per-warp results.  Deterministic for a fixed launch shape.
+__device__ __forceinline__ void block_max_sum(double& mx, double& sm, double* out) {
+    __shared__ double smx[32], ssm[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        sm += __shfl_xor_sync(0xffffffffu, sm, o);
+    }
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nthr = blockDim.x * blockDim.y * blockDim.z;
+    const int w = tid >> 5, l = tid & 31, nw = (nthr + 31) >> 5;
+    if (l == 0) { smx[w] = mx; ssm[w] = sm; }
+    __syncthreads();
+    if (w == 0) {
+        mx = (l < nw) ? smx[l] : 0.0;
+        sm = (l < nw) ? ssm[l] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            sm += __shfl_xor_sync(0xffffffffu, sm, o);
+        }
+        if (l == 0) { out[0] = mx; out[1] = sm; }
+    }
+}
+
+template <typename T, int SYM>
+__global__ void __launch_bounds__(256) k_residual(const T* __restrict__ x, const T* __restrict__ b,
+                                                  const T* __restrict__ C, LevelGeom<T> G, BcTable bc,
+                                                  T* __restrict__ r, double* __restrict__ partials) {
+    AGB_NODE_INDEX
+    double mx = 0.0, sm = 0.0;
+    if (live) {
+        T ax[3];
+        apply_node<T, SYM>(x, C, G, bc, i, j, k, id, ax);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const int64_t q = c * G.N + id;
+            const T rv = b[q] - ax[c];
+            r[q] = rv;
+            const double a = fabs((double)rv);
+            mx = fmax(mx, a);
+            sm += a * a;
+        }
+    }
+    if (partials) {
+        const int blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+        block_max_sum(mx, sm, partials + 2 * blk);
+    }
+}
+
+int residual_blocks(int nx, int ny, int nz) {
+    dim3 g = grid3(nx, ny, nz);
+    return (int)(g.x * g.y * g.z);
+}
+
+template <typename T>
+cudaError_t launch_residual(int sym, const T* x, const T* b, const T* C, const LevelGeom<T>& G, const BcTable& bc,
+                            T* r, double* partials, int* nblocks_out, cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
+    if (nblocks_out) *nblocks_out = (int)(grd.x * grd.y * grd.z);
+    if (sym == SYM_ISO) k_residual<T, SYM_ISO><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
+    else k_residual<T, SYM_MM><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
+    return cudaGetLastError();
+}
+template cudaError_t launch_residual<double>(int, const double*, const double*, const double*,
+                                             const LevelGeom<double>&, const BcTable&, double*, double*, int*,
+                                             cudaStream_t);
+template cudaError_t launch_residual<float>(int, const float*, const float*, const float*, const LevelGeom<float>&,
+                                            const BcTable&, float*, double*, int*, cudaStream_t);
+
+__global__ void __launch_bounds__(1024) k_reduce_norms(const double* __restrict__ p, int nb, double* __restrict__ out) {
+    double mx = 0.0, sm = 0.0;
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+        mx = fmax(mx, p[2 * q]);
+        sm += p[2 * q + 1];
+    }
+    __shared__ double o[2];
+    block_max_sum(mx, sm, o);
+    __syncthreads();
+    if (threadIdx.x == 0) { out[0] = o[0]; out[1] = sqrt(o[1]); }
+}
+
+cudaError_t launch_reduce_norms(const double* partials, int nblocks, double* norms, cudaStream_t s) {
+    k_reduce_norms<<<1, 1024, 0, s>>>(partials, nblocks, norms);
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256) k_vec_partials(const double* __restrict__ v, int64_t n, double* __restrict__ p) {
+    double mx = 0.0, sm = 0.0;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const double a = fabs(v[q]);
+        mx = fmax(mx, a);
+        sm += a * a;
+    }
+    block_max_sum(mx, sm, p + 2 * blockIdx.x);
+}
+
+cudaError_t launch_vec_norms(const double* v, int64_t n, double* partials, int nblocks, double* norms,
+                             cudaStream_t s) {
+    k_vec_partials<<<nblocks, 256, 0, s>>>(v, n, partials);
+    k_reduce_norms<<<1, 1024, 0, s>>>(partials, nblocks, norms);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- transfer
+// Nodal full weighting with boundary-reduced weights
+// (src/Operator/Operator.cpp:294-352): corners injected, edges 1/4-1/2-1/4,
+// faces the 9-point /16 stencil, interior the 27-point 1/8-1/16-1/32-1/64.
+template <typename T, typename F>
+__device__ __forceinline__ T restrict_point(F f, int I, int J, int K, int ncx, int ncy, int ncz) {
+    const bool ex = (I == 0) | (I == ncx - 1), ey = (J == 0) | (J == ncy - 1), ez = (K == 0) | (K == ncz - 1);
+    if (ex & ey & ez) return f(0, 0, 0);
+    if (ey & ez) return T(0.25) * f(-1, 0, 0) + T(0.5) * f(0, 0, 0) + T(0.25) * f(1, 0, 0);
+    if (ez & ex) return T(0.25) * f(0, -1, 0) + T(0.5) * f(0, 0, 0) + T(0.25) * f(0, 1, 0);
+    if (ex & ey) return T(0.25) * f(0, 0, -1) + T(0.5) * f(0, 0, 0) + T(0.25) * f(0, 0, 1);
+    if (ex)
+        return (f(0, -1, -1) + T(2) * f(0, 0, -1) + f(0, 1, -1) + T(2) * f(0, -1, 0) + T(4) * f(0, 0, 0) +
+                T(2) * f(0, 1, 0) + f(0, -1, 1) + T(2) * f(0, 0, 1) + f(0, 1, 1)) * T(1.0 / 16.0);
+    if (ey)
+        return (f(-1, 0, -1) + T(2) * f(-1, 0, 0) + f(-1, 0, 1) + T(2) * f(0, 0, -1) + T(4) * f(0, 0, 0) +
+                T(2) * f(0, 0, 1) + f(1, 0, -1) + T(2) * f(1, 0, 0) + f(1, 0, 1)) * T(1.0 / 16.0);
+    if (ez)
+        return (f(-1, -1, 0) + T(2) * f(0, -1, 0) + f(1, -1, 0) + T(2) * f(-1, 0, 0) + T(4) * f(0, 0, 0) +
+                T(2) * f(1, 0, 0) + f(-1, 1, 0) + T(2) * f(0, 1, 0) + f(1, 1, 0)) * T(1.0 / 16.0);
+    const T corners = f(-1, -1, -1) + f(-1, -1, 1) + f(-1, 1, -1) + f(-1, 1, 1) + f(1, -1, -1) + f(1, -1, 1) +
+                      f(1, 1, -1) + f(1, 1, 1);
+    const T edges = f(0, -1, -1) + f(0, -1, 1) + f(0, 1, -1) + f(0, 1, 1) + f(-1, 0, -1) + f(1, 0, -1) + f(-1, 0, 1) +
+                    f(1, 0, 1) + f(-1, -1, 0) + f(-1, 1, 0) + f(1, -1, 0) + f(1, 1, 0);
+    const T faces = f(-1, 0, 0) + f(0, -1, 0) + f(0, 0, -1) + f(1, 0, 0) + f(0, 1, 0) + f(0, 0, 1);
+    return corners * T(1.0 / 64.0) + edges * T(1.0 / 32.0) + faces * T(1.0 / 16.0) + f(0, 0, 0) * T(1.0 / 8.0);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_restrict(const T* __restrict__ fine, LevelGeom<T> Gf, T* __restrict__ crse,
+                                                  LevelGeom<T> G) {
+    AGB_NODE_INDEX
+    if (!live) return;
+    const int64_t fid = 2 * i + Gf.sy * (2 * j) + Gf.sz * (2 * k);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const T* fc = fine + c * Gf.N + fid;
+        auto f = [&](int a, int b, int d) { return fc[a + Gf.sy * b + Gf.sz * d]; };
+        crse[c * G.N + id] = restrict_point<T>(f, i, j, k, G.nx, G.ny, G.nz);
+    }
+}
+
+template <typename T>
+cudaError_t launch_restrict(const T* fine, const LevelGeom<T>& Gf, T* crse, const LevelGeom<T>& Gc, cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(Gc.nx, Gc.ny, Gc.nz);
+    k_restrict<T><<<grd, blk, 0, s>>>(fine, Gf, crse, Gc);
+    return cudaGetLastError();
+}
+template cudaError_t launch_restrict<double>(const double*, const LevelGeom<double>&, double*,
+                                             const LevelGeom<double>&, cudaStream_t);
+template cudaError_t launch_restrict<float>(const float*, const LevelGeom<float>&, float*, const LevelGeom<float>&,
+                                            cudaStream_t);
+
+// C coarsening (src/Operator/Elastic.cpp:786-834): same weights per entry
+__global__ void __launch_bounds__(256) k_restrict_C(const double* __restrict__ Cf, LevelGeom<double> Gf,
+                                                    double* __restrict__ Cc, LevelGeom<double> G, int nc) {
+    AGB_NODE_INDEX
+    if (!live) return;
+    const int64_t fid = 2 * i + Gf.sy * (2 * j) + Gf.sz * (2 * k);
+    for (int c = 0; c < nc; c++) {
+        const double* fc = Cf + c * Gf.N + fid;
+        auto f = [&](int a, int b, int d) { return fc[a + Gf.sy * b + Gf.sz * d]; };
+        Cc[c * G.N + id] = restrict_point<double>(f, i, j, k, G.nx, G.ny, G.nz);
+    }
+}
+
+cudaError_t launch_restrict_C(const double* Cf, const LevelGeom<double>& Gf, double* Cc, const LevelGeom<double>& Gc,
+                              int nc, cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(Gc.nx, Gc.ny, Gc.nz);
+    k_restrict_C<<<grd, blk, 0, s>>>(Cf, Gf, Cc, Gc, nc);
+    return cudaGetLastError();
+}
+
+// trilinear prolongation added to the fine field
+// (src/Operator/Operator.cpp:399-428)
+template <typename T>
+__global__ void __launch_bounds__(256) k_prolong_add(const T* __restrict__ crse, LevelGeom<T> Gc, T* __restrict__ fine,
+                                                     LevelGeom<T> G) {
+    AGB_NODE_INDEX
+    if (!live) return;
+    const int I = i >> 1, J = j >> 1, K = k >> 1;
+    const int oi = i & 1, oj = j & 1, ok = k & 1;
+    const int64_t cid = I + Gc.sy * J + Gc.sz * K;
+    const int64_t dx = oi, dy = oj ? Gc.sy : 0, dz = ok ? Gc.sz : 0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const T* cc = crse + c * Gc.N + cid;
+        T v;
+        const int odd = oi + oj + ok;
+        if (odd == 0) v = cc[0];
+        else if (odd == 1) v = T(0.5) * (cc[0] + cc[dx + dy + dz]);
+        else if (odd == 2) {
+            // face centre: the two odd directions span the four corners
+            int64_t a, b2;
+            if (!oi) { a = dy; b2 = dz; }
+            else if (!oj) { a = dx; b2 = dz; }
+            else { a = dx; b2 = dy; }
+            v = T(0.25) * (cc[0] + cc[a] + cc[b2] + cc[a + b2]);
+        } else {
+            v = T(0.125) * (cc[0] + cc[dx] + cc[dy] + cc[dz] + cc[dy + dz] + cc[dx + dz] + cc[dx + dy] + cc[dx + dy + dz]);
+        }
+        fine[c * G.N + id] += v;
+    }
+}
+
+template <typename T>
+cudaError_t launch_prolong_add(const T* crse, const LevelGeom<T>& Gc, T* fine, const LevelGeom<T>& Gf,
+                               cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(Gf.nx, Gf.ny, Gf.nz);
+    k_prolong_add<T><<<grd, blk, 0, s>>>(crse, Gc, fine, Gf);
+    return cudaGetLastError();
+}
+template cudaError_t launch_prolong_add<double>(const double*, const LevelGeom<double>&, double*,
+                                                const LevelGeom<double>&, cudaStream_t);
+template cudaError_t launch_prolong_add<float>(const float*, const LevelGeom<float>&, float*, const LevelGeom<float>&,
+                                               cudaStream_t);
+
+// ---------------------------------------------------------------- helpers
+__global__ void k_aos_to_soa(const double* __restrict__ a, double* __restrict__ s, int64_t N, int nc) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < N * nc; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = q / nc;
+        const int c = (int)(q - node * nc);
+        s[c * N + node] = a[q];
+    }
+}
+__global__ void k_soa_to_aos(const double* __restrict__ s, double* __restrict__ a, int64_t N, int nc) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < N * nc; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = q / nc;
+        const int c = (int)(q - node * nc);
+        a[q] = s[c * N + node];
+    }
+}
+cudaError_t launch_aos_to_soa(const double* aos, double* soa, int64_t N, int nc, cudaStream_t s) {
+    k_aos_to_soa<<<flat_blocks(N * nc), 256, 0, s>>>(aos, soa, N, nc);
+    return cudaGetLastError();
+}
+cudaError_t launch_soa_to_aos(const double* soa, double* aos, int64_t N, int nc, cudaStream_t s) {
+    k_soa_to_aos<<<flat_blocks(N * nc), 256, 0, s>>>(soa, aos, N, nc);
+    return cudaGetLastError();
+}
+
+__global__ void k_to_float(const double* __restrict__ in, float* __restrict__ out, int64_t n, double scale) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        out[q] = (float)(in[q] * scale);
+}
+cudaError_t launch_to_float(const double* in, float* out, int64_t n, double scale, cudaStream_t s) {
+    k_to_float<<<flat_blocks(n), 256, 0, s>>>(in, out, n, scale);
+    return cudaGetLastError();
+}
+
+__global__ void k_add_float(const float* __restrict__ in, double* __restrict__ out, int64_t n, double scale) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        out[q] += scale * (double)in[q];
+}
+cudaError_t launch_add_float(const float* in, double* out, int64_t n, double scale, cudaStream_t s) {
+    k_add_float<<<flat_blocks(n), 256, 0, s>>>(in, out, n, scale);
+    return cudaGetLastError();
+}
+
+__global__ void k_axpy(double a, const double* __restrict__ x, double* __restrict__ y, int64_t n) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        y[q] += a * x[q];
+}
+cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStream_t s) {
+    k_axpy<<<flat_blocks(n), 256, 0, s>>>(a, x, y, n);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- BC init
+// BC::Operator::Elastic::Constant::Init (src/BC/Operator/Elastic/Constant.H:
+// 197-286): every boundary node of b gets its region's value (0 for
+// displacement rows when homogeneous).
+__global__ void __launch_bounds__(256) k_bc_init(double* __restrict__ b, LevelGeom<double> G, BcTable bc,
+                                                 const double* __restrict__ val, int homogeneous) {
+    AGB_NODE_INDEX
+    if (!live) return;
+    const int cx = (i == 0) ? -1 : (i == G.nx - 1) ? 1 : 0;
+    const int cy = (j == 0) ? -1 : (j == G.ny - 1) ? 1 : 0;
+    const int cz = (k == 0) ? -1 : (k == G.nz - 1) ? 1 : 0;
+    if (!(cx | cy | cz)) return;
+    double n[3];
+    const int reg = boundary_region<double>(cx, cy, cz, n);
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+        b[d * G.N + id] = (homogeneous && bc.t[reg * 3 + d] == BC_DISP) ? 0.0 : val[reg * 3 + d];
+}
+
+cudaError_t launch_bc_init(double* b, const LevelGeom<double>& G, const BcTable& bc, const double* bcval_dev,
+                           int homogeneous, cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
+    k_bc_init<<<grd, blk, 0, s>>>(b, G, bc, bcval_dev, homogeneous);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- RHS
+__device__ __forceinline__ double f0_at(const double* F0, int f0n, int64_t id, int p, int q) {
+    if (f0n == 1) return p == q ? F0[id] : 0.0;
+    if (f0n == 9) return F0[id * 9 + p * 3 + q];
+    return 0.0;
+}
+
+// dw = C (grad u - F0), stored SoA as 9 components (row-major p*3+q)
+template <int SYM>
+__global__ void __launch_bounds__(256) k_dw(const double* __restrict__ u, const double* __restrict__ F0, int f0n,
+                                            const double* __restrict__ C, LevelGeom<double> G,
+                                            double* __restrict__ dw) {
+    AGB_NODE_INDEX
+    if (!live) return;
+    double g[3][3], s[3][3];
+    grad_at(u, G, i, j, k, id, g);
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) g[p][q] -= f0_at(F0, f0n, id, p, q);
+    const int64_t N = G.N;
+    auto cf = [&](int a) { return C[a * N + id]; };
+    stress_of<double, SYM>(cf, g, s);
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) dw[(p * 3 + q) * N + id] = s[p][q];
+}
+
+__global__ void __launch_bounds__(256) k_rhs(const double* __restrict__ u, const double* __restrict__ b,
+                                             const double* __restrict__ dw, LevelGeom<double> G, BcTable bc,
+                                             double* __restrict__ rhs) {
+    AGB_NODE_INDEX
+    if (!live) return;
+    const int64_t N = G.N;
+    const int cx = (i == 0) ? -1 : (i == G.nx - 1) ? 1 : 0;
+    const int cy = (j == 0) ? -1 : (j == G.ny - 1) ? 1 : 0;
+    const int cz = (k == 0) ? -1 : (k == G.nz - 1) ? 1 : 0;
+    double ret[3];
+    if (cx | cy | cz) {
+        double g[3][3], s[3][3], n[3];
+        grad_at(u, G, i, j, k, id, g);
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) s[p][q] = dw[(p * 3 + q) * N + id];
+        const int reg = boundary_region<double>(cx, cy, cz, n);
+#pragma unroll
+        for (int r = 0; r < 3; r++) ret[r] = bc_component<double>(bc, reg, r, u[r * N + id], g, s, n);
+    } else {
+        // div dw with central differences (src/Numeric/Stencil.H:588-657)
+        const int64_t off[3] = {1, G.sy, G.sz};
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            double acc = 0.0;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                const double* w = dw + (c * 3 + d) * N + id;
+                acc += (w[off[d]] - w[-off[d]]) * G.h[d];
+            }
+            ret[c] = acc;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) rhs[c * N + id] = b[c * N + id] - ret[c];
+}
+
+cudaError_t launch_build_rhs(int sym, const double* u, const double* b, const double* F0, int f0_ncomp,
+                             const double* C, const LevelGeom<double>& G, const BcTable& bc, double* dw, double* rhs,
+                             cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
+    if (sym == SYM_ISO) k_dw<SYM_ISO><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
+    else k_dw<SYM_MM><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_rhs<<<grd, blk, 0, s>>>(u, b, dw, G, bc, rhs);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- stress
+template <int SYM>
+__global__ void __launch_bounds__(256) k_stress_strain(const double* __restrict__ u, const double* __restrict__ F0,
+                                                       int f0n, const double* __restrict__ C, LevelGeom<double> G,
+                                                       double* __restrict__ stress, double* __restrict__ strain,
+                                                       double* __restrict__ energy) {
+    AGB_NODE_INDEX
+    if (!live) return;
+    double g[3][3], ge[3][3], s[3][3];
+    grad_at(u, G, i, j, k, id, g);
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) ge[p][q] = g[p][q] - f0_at(F0, f0n, id, p, q);
+    const int64_t N = G.N;
+    auto cf = [&](int a) { return C[a * N + id]; };
+    stress_of<double, SYM>(cf, ge, s);
+    double en = 0.0;
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const double e = 0.5 * (g[p][q] + g[q][p]);
+            if (stress) stress[id * 9 + p * 3 + q] = s[p][q];
+            if (strain) strain[id * 9 + p * 3 + q] = e;
+            en += 0.5 * s[p][q] * e;
+        }
+    if (energy) energy[id] = en;
+}
+
+cudaError_t launch_stress_strain(int sym, const double* u, const double* F0, int f0_ncomp, const double* C,
+                                 const LevelGeom<double>& G, double* stress, double* strain, double* energy,
+                                 cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
+    if (sym == SYM_ISO) k_stress_strain<SYM_ISO><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, stress, strain, energy);
+    else k_stress_strain<SYM_MM><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, stress, strain, energy);
+    return cudaGetLastError();
+}
+
+}  // namespace agb

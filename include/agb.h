@@ -1,0 +1,234 @@
+/*
+ * agb.h — C ABI of alamo_gb300, a GB300 (sm_103a) implementation of alamo's
+ * nodal linear-elastic multigrid path: the Operator::Elastic stencil
+ * (Fapply), its damped-Jacobi smoother (Fsmooth), the operator diagonal, the
+ * residual, nodal restriction/prolongation, the per-level stiffness
+ * coarsening, the Newton right-hand side and the multigrid V-cycle solve
+ * behind Solver::Nonlocal::Linear, plus an FP32-cycle / FP64-refinement
+ * mixed-precision solve.
+ *
+ * Every entry point replaces a reference interface (file:line inside the
+ * reference project Gopal-B/alamo) cited beside it.  Conventions:
+ *   - one handle = one single-level uniform node grid nx*ny*nz on one GPU
+ *     (the current CUDA device when the handle is created);
+ *   - node fields are float64, x fastest, no ghost nodes; vector fields are
+ *     3 components stored one after another (SoA: comp*N + node);
+ *   - stiffness per node in the reference's object layout (AoS):
+ *     isotropic {lambda, mu}; major-minor the 21 entries data[0..20] of
+ *     Set::Matrix4<3,MajorMinor> (src/Set/Matrix4_MajorMinor.H:327-375);
+ *   - `where` says whether array arguments are host (AGB_MEM_HOST) or device
+ *     (AGB_MEM_DEVICE) pointers; host arrays are copied in and out;
+ *   - calls return when their work is complete; they never abort or trap:
+ *     errors come back as agb_status, with detail in agb_last_error().
+ *   - a handle is not re-entrant; use one handle per host thread.
+ */
+#ifndef AGB_H
+#define AGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    AGB_OK = 0,
+    AGB_NOT_CONVERGED = 1, /* iteration cap reached (MLMG's throw, Linear.H:137-146) */
+    AGB_NAN = 2,           /* NaN in a residual or the solution (Elastic.cpp:262-286, Linear.H:122-126) */
+    AGB_BAD_ARG = 3,       /* inconsistent sizes, null pointers, unknown enum values */
+    AGB_CUDA_ERROR = 4,    /* a CUDA call failed; see agb_last_error() */
+    AGB_NOT_READY = 5,     /* model or boundary condition not set (Elastic.H:127) */
+    AGB_OUT_OF_MEMORY = 6,
+    AGB_LIMIT = 7          /* request beyond a documented size limit */
+} agb_status;
+
+typedef enum { AGB_SYM_ISOTROPIC = 0, AGB_SYM_MAJORMINOR = 1 } agb_sym;
+typedef enum { AGB_MEM_HOST = 0, AGB_MEM_DEVICE = 1 } agb_mem;
+/* BC::Operator::Elastic::Elastic::Type (src/BC/Operator/Elastic/Elastic.H:26) */
+typedef enum {
+    AGB_BC_DISPLACEMENT = 0,
+    AGB_BC_TRACTION = 1,
+    AGB_BC_PERIODIC = 2,
+    AGB_BC_NEUMANN = 3,
+    AGB_BC_NONE = 4
+} agb_bc_type;
+typedef enum { AGB_PRECISION_FP64 = 0, AGB_PRECISION_MIXED = 1 } agb_precision;
+
+/* Solver settings; field names follow the reference's `solver.*` keys
+ * (Solver::Nonlocal::Linear::Parse, src/Solver/Nonlocal/Linear.H:296-382). */
+typedef struct agb_solver_opts {
+    int max_iter;             /* V-cycles before AGB_NOT_CONVERGED (200) */
+    int pre_smooth;           /* Fsmooth calls before restriction (2) */
+    int post_smooth;          /* Fsmooth calls after prolongation (2) */
+    int final_smooth;         /* Fsmooth calls after a failed bottom solve (8) */
+    int bottom_smooth;        /* Fsmooth calls after a good bottom solve (0) */
+    int bottom_max_iter;      /* BiCGStab iterations on the coarsest level (200) */
+    double bottom_tol_rel;    /* (1e-4) */
+    double bottom_tol_abs;    /* (-1: off) */
+    double omega;             /* Jacobi damping, Operator.H:123 (2/3) */
+    int max_coarsening_level; /* -1: coarsen while every axis keeps >= 2 cells */
+    int fixed_iter;           /* > 0: run exactly this many cycles */
+    int verbose;
+    int precision;            /* agb_precision (AGB_PRECISION_FP64) */
+    int inner_cycles;         /* mixed: FP32 V-cycles per FP64 residual (1) */
+} agb_solver_opts;
+
+typedef struct agb_solve_report {
+    int status;               /* agb_status of the solve */
+    int iters;                /* V-cycles (FP32 cycles in mixed precision) */
+    int nlevels;
+    int bottom_iters;         /* BiCGStab iterations summed over cycles (last read) */
+    int fp64_residuals;       /* FP64 fine-level residual evaluations */
+    int reserved;
+    double resnorm0;          /* ||rhs - A x0||_inf */
+    double rhsnorm0;          /* ||rhs||_inf */
+    double final_resnorm;     /* ||rhs - A x||_inf at exit (FP64) */
+    double final_resnorm_l2;  /* ||rhs - A x||_2 at exit (FP64) */
+    double rhsnorm_l2;        /* ||rhs||_2 */
+    double seconds;           /* wall time of the call */
+} agb_solve_report;
+
+typedef struct agb_elastic agb_elastic;
+
+/* ---------------------------------------------------------------- set-up */
+agb_status agb_default_opts(agb_solver_opts* opts);
+
+/* Operator::Elastic<SYM>::Elastic / define (src/Operator/Elastic.cpp:10-55)
+ * with the multigrid hierarchy of Operator<Grid::Node>::define
+ * (src/Operator/Operator.cpp:185-228) and Solver::Nonlocal::Linear::Define
+ * (src/Solver/Nonlocal/Linear.H:36-43).  nx, ny, nz >= 3 nodes; dx = cell
+ * size per axis; opts may be NULL for defaults. */
+agb_status agb_elastic_create(agb_elastic** h, int nx, int ny, int nz, const double dx[3], int sym,
+                              const agb_solver_opts* opts);
+agb_status agb_elastic_destroy(agb_elastic* h);
+/* Linear::set* / PrepareMLMG (src/Solver/Nonlocal/Linear.H:170-178, 255-290) */
+agb_status agb_elastic_set_opts(agb_elastic* h, const agb_solver_opts* opts);
+/* run on a caller's cudaStream_t (NULL: the handle's own stream) */
+agb_status agb_elastic_set_stream(agb_elastic* h, void* cuda_stream);
+/* Elastic::SetModel (src/Operator/Elastic.cpp:87-116): per-node stiffness,
+ * 2 (isotropic) or 21 (major-minor) doubles per node, AoS. */
+agb_status agb_elastic_set_model(agb_elastic* h, const double* C, int where);
+/* read back the (coarsened) stiffness of a multigrid level, AoS */
+agb_status agb_elastic_get_model(agb_elastic* h, int level, double* C, int where);
+/* Elastic::SetBC (src/Operator/Elastic.H:61-65) with the tables of
+ * BC::Operator::Elastic::Constant (src/BC/Operator/Elastic/Constant.H:
+ * 435-436): type[26*3] (agb_bc_type) and val[26*3], region order of the
+ * Face enum (src/BC/Operator/Elastic/Elastic.H:35-43). */
+agb_status agb_elastic_set_bc(agb_elastic* h, const int* type, const double* val);
+/* Operator<Grid::Node>::prepareForSolve (src/Operator/Operator.cpp:253-260):
+ * stiffness on all levels (Elastic::averageDownCoeffsSameAmrLevel,
+ * src/Operator/Elastic.cpp:746-836) and the diagonal of every level.  Called
+ * implicitly by the solves after set_model / set_bc / set_opts. */
+agb_status agb_elastic_prepare(agb_elastic* h);
+agb_status agb_elastic_num_levels(agb_elastic* h, int* nlevels);
+agb_status agb_elastic_level_dims(agb_elastic* h, int level, int dims[3]);
+
+/* ------------------------------------------------------ operator hooks */
+/* Elastic<SYM>::Fapply (src/Operator/Elastic.cpp:139-292): f = A u on a
+ * multigrid level.  u, f: 3*N doubles of that level. */
+agb_status agb_elastic_fapply(agb_elastic* h, int level, const double* u, double* f, int where);
+/* the same operator evaluated in FP32 arithmetic (the mixed solve's cycle) */
+agb_status agb_elastic_fapply_f32(agb_elastic* h, int level, const float* u, float* f, int where);
+/* Elastic<SYM>::Diagonal (src/Operator/Elastic.cpp:296-379) */
+agb_status agb_elastic_diagonal(agb_elastic* h, int level, double* diag, int where);
+/* Operator<Grid::Node>::Fsmooth (src/Operator/Operator.cpp:88-154): each call
+ * is two damped-Jacobi sweeps x <- (1-w) x + w (b - (Ax - Dx)) / D. */
+agb_status agb_elastic_fsmooth(agb_elastic* h, int level, double* x, const double* b, int ncalls, int where);
+/* Operator<Grid::Node>::solutionResidual / correctionResidual
+ * (src/Operator/Operator.cpp:635-657): r = b - A x; norms (may be NULL)
+ * receives {||r||_inf, ||r||_2}. */
+agb_status agb_elastic_residual(agb_elastic* h, int level, const double* x, const double* b, double* r,
+                                double norms[2], int where);
+/* Operator<Grid::Node>::restriction (src/Operator/Operator.cpp:262-363):
+ * fine field of level crse_level-1 -> coarse field of level crse_level */
+agb_status agb_elastic_restrict(agb_elastic* h, int crse_level, const double* fine, double* crse, int where);
+/* Operator<Grid::Node>::interpolation (src/Operator/Operator.cpp:365-434):
+ * fine (level fine_level) += P crse (level fine_level+1) */
+agb_status agb_elastic_prolong_add(agb_elastic* h, int fine_level, const double* crse, double* fine, int where);
+
+/* ------------------------------------------------------------- solves */
+/* BC::Operator::Elastic::Constant::Init (src/BC/Operator/Elastic/
+ * Constant.H:197-286): boundary values of the BC table into b (3*N). */
+agb_status agb_elastic_bc_init(agb_elastic* h, double* b, int homogeneous, int where);
+/* Newton::prepareForSolve right-hand side (src/Solver/Nonlocal/Newton.H:
+ * 144-231): rhs = b - div(C (grad u - F0)) inside, b - BC(u, grad u,
+ * C (grad u - F0)) on the boundary.  F0: NULL (f0_ncomp 0), one value per
+ * node for F0 = s I (f0_ncomp 1) or 9 row-major values per node (9). */
+agb_status agb_elastic_build_rhs(agb_elastic* h, const double* u, const double* b, const double* F0, int f0_ncomp,
+                                 double* rhs, int where);
+/* Solver::Nonlocal::Linear::solve (src/Solver/Nonlocal/Linear.H:131-147):
+ * V-cycles on A sol = rhs from the initial guess in sol until
+ * ||rhs - A sol||_inf <= max(tol_abs, tol_rel * max(||rhs||_inf, ||r0||_inf)).
+ * opts.precision selects the plain FP64 cycle or FP32 cycles inside FP64
+ * iterative refinement.  rep may be NULL. */
+agb_status agb_linear_solve(agb_elastic* h, double* sol, const double* rhs, double tol_rel, double tol_abs,
+                            agb_solve_report* rep, int where);
+/* Solver::Nonlocal::Newton::solve with nriters = 1 (src/Solver/Nonlocal/
+ * Newton.H:279-358) for a linear model with eigenstrain F0: builds the RHS
+ * at u, solves for the increment and adds it to u. */
+agb_status agb_newton_solve(agb_elastic* h, double* u, const double* b, const double* F0, int f0_ncomp,
+                            double tol_rel, double tol_abs, agb_solve_report* rep, int where);
+/* Stress / strain / energy after a solve (src/Integrator/Base/Mechanics.H:
+ * 210-248, src/Operator/Elastic.cpp:426-603): stress = C (grad u - F0),
+ * strain = sym grad u, 9 row-major values per node; energy = sigma:eps / 2.
+ * Outputs may be NULL. */
+agb_status agb_elastic_stress_strain(agb_elastic* h, const double* u, const double* F0, int f0_ncomp,
+                                     double* stress, double* strain, double* energy, int where);
+
+/* --------------------------------------------------------- profiling */
+/* Kernel families timed with CUDA events on the handle's stream when
+ * profiling is on (fine level only). */
+typedef enum {
+    AGB_K_FAPPLY_F64 = 0,
+    AGB_K_JACOBI_F64 = 1,
+    AGB_K_RESIDUAL_F64 = 2,
+    AGB_K_FAPPLY_F32 = 3,
+    AGB_K_JACOBI_F32 = 4,
+    AGB_K_RESIDUAL_F32 = 5,
+    AGB_K_RESTRICT = 6,
+    AGB_K_PROLONG = 7,
+    AGB_K_BOTTOM = 8,
+    AGB_K_NFAMILIES = 9
+} agb_kernel_family;
+agb_status agb_profile_enable(agb_elastic* h, int on);
+agb_status agb_profile_reset(agb_elastic* h);
+/* launches and summed device milliseconds of one family since the reset */
+agb_status agb_profile_get(agb_elastic* h, int family, int64_t* launches, double* ms);
+/* kernels of this library launched since the handle was created */
+agb_status agb_launch_count(agb_elastic* h, int64_t* launches);
+
+/* ------------------------------------------------ synthetic inputs */
+/* Set::Matrix4<3,MajorMinor>::Cubic(C11, C12, C44, R)
+ * (src/Set/Matrix4_MajorMinor.H:518-547), R row-major. */
+agb_status agb_cubic_stiffness(double C11, double C12, double C44, const double R[9], double out21[21]);
+/* Uniform doubles in [lo, hi) from std::mt19937_64(seed) (53-bit mantissa). */
+agb_status agb_synth_uniform(uint64_t seed, int64_t n, double lo, double hi, double* out);
+/* One spherical inclusion: nodes x = (i,j,k) dx with |x - center| < radius
+ * get (lam_in, mu_in) and F0 = eps_in I, others (lam_out, mu_out), F0 = 0.
+ * C: 2 doubles per node; F0s: 1 double per node (may be NULL). */
+agb_status agb_synth_inclusion_iso(int nx, int ny, int nz, const double dx[3], const double center[3], double radius,
+                                   double lam_in, double mu_in, double lam_out, double mu_out, double eps_in,
+                                   double* C, double* F0s);
+/* Voronoi polycrystal: nseeds seeds uniform in the box, each node belongs to
+ * its nearest seed; every grain gets the cubic stiffness rotated by a
+ * Haar-uniform rotation (unit quaternion from 4 normals).  C: 21 doubles per
+ * node (AoS); grain (may be NULL): grain id per node. */
+agb_status agb_synth_voronoi_cubic(int nx, int ny, int nz, const double dx[3], int nseeds, uint64_t seed, double C11,
+                                   double C12, double C44, double* C, int32_t* grain);
+/* Non-overlapping spheres (rejection sampling): radius uniform in
+ * [rmin, rmax], centres uniform in the box, inclusion (lam_in, mu_in) with
+ * dilatational eigenstrain s uniform in [smin, smax]; matrix
+ * (lam_out, mu_out).  placed receives the number of spheres placed. */
+agb_status agb_synth_spheres_iso(int nx, int ny, int nz, const double dx[3], int nspheres, uint64_t seed, double rmin,
+                                 double rmax, double lam_in, double mu_in, double lam_out, double mu_out, double smin,
+                                 double smax, double* C, double* F0s, int* placed);
+
+const char* agb_status_string(int status);
+const char* agb_last_error(void);
+const char* agb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AGB_H */

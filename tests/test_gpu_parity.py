@@ -1,0 +1,312 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle.
+
+Bar: FP64 operator-level results within 1e-12 relative (inf-norm of the
+difference over inf-norm of the oracle's result); solved displacement within
+1e-8 relative; FP32 operator within 2e-6 relative.  Inputs are the seeded
+synthetic fields of the benchmark configurations at sizes the oracle handles
+in seconds; full-size cases check size-independent properties.
+"""
+import numpy as np
+import pytest
+
+import problems as P
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+
+
+def rel(a, b):
+    d = np.abs(np.asarray(a) - np.asarray(b)).max()
+    s = np.abs(np.asarray(b)).max()
+    return d / s if s > 0 else d
+
+
+def make_op(agb, C, bc, dx, **kw):
+    n = C.shape[2], C.shape[1], C.shape[0]
+    op = agb.Elastic(n, dx, "isotropic" if C.shape[-1] == 2 else "majorminor", agb.default_opts(**kw))
+    op.SetModel(np.ascontiguousarray(C))
+    op.SetBC(bc)
+    return op
+
+
+CASES = {
+    "c1-iso": lambda: P.c1(33),
+    "voronoi-mm": lambda: P.voronoi_clamp(33),
+    "iso-randbc": lambda: (P.c1(17)[0], None, P.random_bc(11), P.c1(17)[3]),
+    "mm-randbc": lambda: (P.voronoi_clamp(17)[0], None, P.random_bc(12), P.voronoi_clamp(17)[3]),
+}
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_fapply_parity(agb, oracle, case):
+    C, F0, bc, dx = CASES[case]()
+    n = C.shape[0]
+    u = P.random_field((3, n, n, n))
+    with make_op(agb, C, bc, dx) as op:
+        f = op.Fapply(u)
+    bt, _ = bc.tables()
+    ref = oracle.fapply(C, bt, u, dx)
+    assert rel(f, ref) <= TOL64
+    # boundary rows on their own scale
+    m = np.zeros((n, n, n), bool)
+    m[0, :, :] = m[-1, :, :] = m[:, 0, :] = m[:, -1, :] = m[:, :, 0] = m[:, :, -1] = True
+    assert rel(f[:, m], ref[:, m]) <= TOL64
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_fapply_f32_parity(agb, oracle, case):
+    C, F0, bc, dx = CASES[case]()
+    n = C.shape[0]
+    u = P.random_field((3, n, n, n))
+    with make_op(agb, C, bc, dx) as op:
+        f = op.Fapply_f32(u.astype(np.float32))
+    bt, _ = bc.tables()
+    assert rel(f, oracle.fapply(C, bt, u, dx)) <= 2e-6
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_coefficients_and_diagonal_all_levels(agb, oracle, case):
+    C, F0, bc, dx = CASES[case]()
+    bt, _ = bc.tables()
+    with make_op(agb, C, bc, dx) as op:
+        op.prepareForSolve()
+        Cl, dxl = C, dx
+        for lev in range(op.num_levels()):
+            if lev > 0:
+                Cl = oracle.restrict_C(Cl)
+                dxl = 2 * dxl
+            assert rel(op.GetModel(lev), Cl) <= TOL64
+            assert rel(op.Diagonal(lev), oracle.diagonal(Cl, bt, dxl)) <= TOL64
+
+
+def test_transfer_parity(agb, oracle):
+    C, F0, bc, dx = P.c1(33)
+    with make_op(agb, C, bc, dx) as op:
+        fine = P.random_field((3, 33, 33, 33), 5)
+        crse = P.random_field((3, 17, 17, 17), 6)
+        assert rel(op.restriction(1, fine), oracle.restrict(fine)) <= TOL64
+        assert rel(op.interpolation(0, fine.copy(), crse), oracle.prolong_add(crse, fine)) <= TOL64
+
+
+@pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm", "mm-randbc"])
+def test_fsmooth_and_residual_parity(agb, oracle, case):
+    C, F0, bc, dx = CASES[case]()
+    n = C.shape[0]
+    bt, _ = bc.tables()
+    x0 = P.random_field((3, n, n, n), 21)
+    b = P.random_field((3, n, n, n), 22)
+    with make_op(agb, C, bc, dx) as op:
+        x = op.Fsmooth(x0.copy(), b, ncalls=2)
+        r, (rinf, r2) = op.residual(x0, b)
+    dg = oracle.diagonal(C, bt, dx)
+    xr = oracle.fsmooth(C, bt, dg, x0, b, dx, ncalls=2)
+    assert rel(x, xr) <= 1e-11
+    rr, rn = oracle.residual(C, bt, x0, b, dx)
+    assert rel(r, rr) <= TOL64
+    assert abs(rinf - rn) <= TOL64 * rn
+    assert abs(r2 - np.sqrt((rr ** 2).sum())) <= 1e-10 * r2
+
+
+@pytest.mark.parametrize("f0kind", ["none", "scalar", "full"])
+def test_bc_init_and_rhs_parity(agb, oracle, f0kind):
+    C, F0, _, dx = P.c1(17)
+    bc = P.random_bc(31)
+    n = 17
+    bt, bv = bc.tables()
+    if f0kind == "none":
+        F0 = None
+    elif f0kind == "full":
+        F0 = P.random_field((n, n, n, 3, 3), 32) * 0.01
+    u = P.random_field((3, n, n, n), 33) * 0.1
+    bbody = P.random_field((3, n, n, n), 34)
+    with make_op(agb, C, bc, dx) as op:
+        b = op.bc_init(bbody.copy())
+        rhs = op.build_rhs(u, b, F0)
+        s, e, en = op.stress_strain(u, F0)
+    bref = oracle.bc_init(bbody, bt, bv)
+    assert np.array_equal(b, bref)
+    F0o = None if F0 is None else (F0 if F0.ndim == 3 else F0.reshape(n, n, n, 9))
+    assert rel(rhs, oracle.build_rhs(C, F0o, bt, u, bref, dx)) <= TOL64
+    so, eo, eno = oracle.stress_strain(C, F0o, u, dx)
+    assert rel(s.reshape(n, n, n, 9), so) <= TOL64
+    assert rel(e.reshape(n, n, n, 9), eo) <= TOL64
+    assert rel(en, eno) <= 1e-11
+
+
+def newton_problem(agb, oracle, C, F0, bc, dx):
+    n = C.shape[0]
+    bt, bv = bc.tables()
+    u0 = np.zeros((3, n, n, n))
+    b = oracle.bc_init(u0, bt, bv)
+    rhs = oracle.build_rhs(C, F0, bt, u0, b, dx)
+    return u0, b, rhs, bt
+
+
+@pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
+def test_vcycle_iterates_match(agb, oracle, case):
+    """Three V-cycles from zero: the GPU iterate equals the oracle's."""
+    C, F0, bc, dx = CASES[case]()
+    u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
+    xo, rep_o, hist_o = oracle.solve(C, bt, rhs, dx, fixed_iter=3)
+    with make_op(agb, C, bc, dx, fixed_iter=3) as op:
+        x = u0.copy()
+        rep = agb.Linear(op).solve(x, rhs, 1e-30, 0.0)
+    assert rep["iters"] == 3
+    assert rel(x, xo) <= 1e-10
+
+
+@pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
+def test_solve_parity(agb, oracle, case):
+    C, F0, bc, dx = CASES[case]()
+    u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
+    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-12)
+    assert rep_o.status == 0
+    with make_op(agb, C, bc, dx) as op:
+        u = u0.copy()
+        rep = agb.Newton(op).solve(u, b, F0, tol_rel=1e-12, tol_abs=0.0)
+    assert rep["status"] == 0 and abs(rep["iters"] - rep_o.iters) <= 1
+    assert rep["final_resnorm"] <= 1e-12 * rep["rhsnorm0"]
+    assert rel(u, xo) <= 1e-8
+
+
+@pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
+def test_mixed_precision_solve(agb, oracle, case):
+    C, F0, bc, dx = CASES[case]()
+    u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
+    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-12)
+    with make_op(agb, C, bc, dx, precision=1) as op:
+        u = u0.copy()
+        rep = agb.Newton(op).solve(u, b, F0, tol_rel=1e-10, tol_abs=0.0)
+    assert rep["status"] == 0
+    # the FP64 outer residual is what the tolerance is checked on
+    assert rep["final_resnorm"] <= 1e-10 * rep["rhsnorm0"]
+    assert rel(u, xo) <= 1e-7
+
+
+def test_uniaxial_known_answer_gpu(agb):
+    from test_oracle_golden import uniaxial_problem
+    n = 33
+    C, bc, dx, E = uniaxial_problem(n)
+    with make_op(agb, C, bc, dx) as op:
+        u = np.zeros((3, n, n, n))
+        b = op.bc_init()
+        agb.Newton(op).solve(u, b, None, tol_rel=1e-10, tol_abs=0.0)
+        s = op.Stress(u)
+    xs = -8 + dx * np.arange(n)
+    ex = (xs + 8) * 0.1 / 16
+    ux = u[0, n // 2, n // 2, :]
+    assert np.sum((ex - ux) ** 2) / np.sum(ex ** 2) < 1e-8
+    sig = s[n // 2, n // 2, :, 0, 0]
+    assert np.sum((sig - E * 0.1 / 16) ** 2) / (n * (E * 0.1 / 16) ** 2) < 1e-8
+
+
+# ------------------------------------------------------------ edge cases
+def test_non_cubic_grid(agb, oracle):
+    C, _ = P.voronoi_clamp(33)[0], None
+    C = np.ascontiguousarray(C[:9, :17, :33])  # nz=9, ny=17, nx=33
+    bc = P.random_bc(40)
+    dx = np.array([1 / 32, 1 / 16, 1 / 8])
+    u = P.random_field((3, 9, 17, 33), 41)
+    with make_op(agb, C, bc, dx) as op:
+        assert op.num_levels() == 3
+        f = op.Fapply(u)
+        op.prepareForSolve()
+        bt, _ = bc.tables()
+        assert rel(op.Diagonal(2), oracle.diagonal(oracle.restrict_C(oracle.restrict_C(C)), bt, 4 * dx)) <= TOL64
+    assert rel(f, oracle.fapply(C, bc.tables()[0], u, dx)) <= TOL64
+
+
+def test_minimal_grid_and_no_coarsening(agb, oracle):
+    C, F0, bc, dx = P.c1(3)
+    u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
+    with make_op(agb, C, bc, dx) as op:
+        assert op.num_levels() == 1
+        x = u0.copy()
+        agb.Linear(op).solve(x, rhs, 1e-12, 0.0)
+    xo, _, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-12)
+    assert rel(x, xo) <= 1e-8
+    C, F0, bc, dx = P.c1(9)
+    u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
+    with make_op(agb, C, bc, dx, max_coarsening_level=0) as op:
+        assert op.num_levels() == 1
+        x = u0.copy()
+        agb.Linear(op).solve(x, rhs, 1e-11, 0.0)
+    xo, _, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-12, max_coarsening_level=0)
+    assert rel(x, xo) <= 1e-8
+
+
+def test_status_codes(agb):
+    from alamo_gb300 import _lib
+    C, F0, bc, dx = P.c1(17)
+    op = agb.Elastic(17, dx)
+    with pytest.raises(agb.AgbError) as ei:
+        agb.Linear(op).solve(np.zeros((3, 17, 17, 17)), np.ones((3, 17, 17, 17)), 1e-8, 0.0)
+    assert ei.value.status == _lib.AGB_NOT_READY
+    op.SetModel(C)
+    rhs = np.ones((3, 17, 17, 17))
+    with pytest.raises(agb.AgbError) as ei:
+        op.SetOpts(agb.default_opts(max_iter=1))
+        agb.Linear(op).solve(np.zeros_like(rhs), rhs, 1e-12, 0.0)
+    assert ei.value.status == _lib.AGB_NOT_CONVERGED
+    Cn = C.copy()
+    Cn[8, 8, 8, 0] = np.nan
+    op.SetOpts(agb.default_opts())
+    op.SetModel(Cn)
+    with pytest.raises(agb.AgbError) as ei:
+        agb.Linear(op).solve(np.zeros_like(rhs), rhs, 1e-12, 0.0)
+    assert ei.value.status == _lib.AGB_NAN
+    op.close()
+
+
+def test_device_pointers_match_host(agb):
+    torch = pytest.importorskip("torch")
+    C, F0, bc, dx = P.voronoi_clamp(33)
+    u = P.random_field((3, 33, 33, 33), 50)
+    with make_op(agb, C, bc, dx) as op:
+        fh = op.Fapply(u)
+        ud = torch.from_numpy(u).cuda()
+        fd = torch.empty_like(ud)
+        op.Fapply(agb.DevicePtr(ud.data_ptr()), agb.DevicePtr(fd.data_ptr()))
+        torch.cuda.synchronize()
+    assert np.array_equal(fh, fd.cpu().numpy())
+
+
+@pytest.mark.slow
+def test_full_size_linearity_257(agb):
+    """A(a u + b v) = a A u + b A v on the 257^3 polycrystal (no races, no
+    out-of-range reads at full size)."""
+    torch = pytest.importorskip("torch")
+    n = 257
+    C, dx = __import__("alamo_gb300").synth.voronoi_cubic(n, 64, seed=1)
+    bc = P.random_bc(60)
+    with make_op(agb, C, bc, dx) as op:
+        del C
+        g = torch.Generator(device="cuda").manual_seed(1)
+        u = torch.rand((3, n, n, n), dtype=torch.float64, device="cuda", generator=g) - 0.5
+        v = torch.rand((3, n, n, n), dtype=torch.float64, device="cuda", generator=g) - 0.5
+        w = 0.75 * u - 1.25 * v
+        fu, fv, fw = torch.empty_like(u), torch.empty_like(u), torch.empty_like(u)
+        for a, f in [(u, fu), (v, fv), (w, fw)]:
+            op.Fapply(agb.DevicePtr(a.data_ptr()), agb.DevicePtr(f.data_ptr()))
+        torch.cuda.synchronize()
+        err = (fw - (0.75 * fu - 1.25 * fv)).abs().max().item() / fw.abs().max().item()
+    assert err <= 1e-12
+
+
+@pytest.mark.slow
+def test_mixed_matches_fp64_129(agb):
+    """Mixed-precision and FP64 solves of the 129^3 sphere medium agree to
+    the solve tolerance's scale."""
+    from alamo_gb300 import synth
+    C, F0, dx, _ = synth.spheres_iso(129, 30, seed=3, rmin=0.05, rmax=0.12)
+    bc = __import__("alamo_gb300").bc.Constant()
+    sols = []
+    for prec in (0, 1):
+        with make_op(agb, C, bc, dx, precision=prec) as op:
+            u = np.zeros((3, 129, 129, 129))
+            b = op.bc_init()
+            rep = agb.Newton(op).solve(u, b, F0, tol_rel=1e-10, tol_abs=0.0)
+            assert rep["status"] == 0
+            sols.append(u)
+    assert rel(sols[1], sols[0]) <= 1e-7

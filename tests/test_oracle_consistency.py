@@ -1,0 +1,63 @@
+"""Internal consistency of the oracle (CPU): the diagonal equals the operator
+probed with unit vectors, isotropic stiffness written as 21 major-minor
+entries gives the same operator, the transfer operators reproduce the
+fields they must, and the V-cycle converges on config 1."""
+import numpy as np
+import pytest
+
+import problems as P
+
+
+def test_diagonal_equals_probed_operator(oracle):
+    n = 7
+    C, F0, bc, dx = P.c1(n)
+    for bcobj in [bc, P.random_bc(3)]:
+        bt, _ = bcobj.tables()
+        dg = oracle.diagonal(C, bt, dx)
+        probe = np.zeros((3, n, n, n))
+        # probe every node/component separately (small grid)
+        for c in range(3):
+            for k in range(n):
+                for j in range(n):
+                    for i in range(n):
+                        e = np.zeros((3, n, n, n))
+                        e[c, k, j, i] = 1.0
+                        probe[c, k, j, i] = oracle.fapply(C, bt, e, dx)[c, k, j, i]
+        assert np.allclose(dg, probe, rtol=1e-13, atol=1e-13 * np.abs(dg).max())
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_isotropic_as_majorminor_same_operator(oracle, seed):
+    n = 9
+    C, _, _, dx = P.c1(n)
+    C = C * (1 + 0.3 * P.random_field((n, n, n, 2), seed))
+    bt, _ = P.random_bc(seed).tables()
+    u = P.random_field((3, n, n, n), seed + 10)
+    f_iso = oracle.fapply(C, bt, u, dx)
+    f_mm = oracle.fapply(np.ascontiguousarray(P.iso_as_mm(C)), bt, u, dx)
+    assert np.abs(f_iso - f_mm).max() <= 1e-12 * np.abs(f_iso).max()
+
+
+def test_transfer_operators(oracle):
+    n = 17
+    x = np.linspace(0, 1, n)
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    lin = np.stack([1 + X + 2 * Y - Z, X * 0 + 3, 2 * Z - Y])
+    c = oracle.restrict(lin)
+    xc = np.linspace(0, 1, 9)
+    Zc, Yc, Xc = np.meshgrid(xc, xc, xc, indexing="ij")
+    assert np.allclose(c, np.stack([1 + Xc + 2 * Yc - Zc, Xc * 0 + 3, 2 * Zc - Yc]), atol=1e-14)
+    fine = oracle.prolong_add(c, np.zeros_like(lin))
+    assert np.allclose(fine, lin, atol=1e-14)
+
+
+def test_vcycle_converges_config1(oracle):
+    C, F0, bc, dx = P.c1(17)
+    bt, bv = bc.tables()
+    n = 17
+    u = np.zeros((3, n, n, n))
+    b = oracle.bc_init(u, bt, bv)
+    rhs = oracle.build_rhs(C, F0, bt, u, b, dx)
+    x, rep, hist = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10)
+    assert rep.status == 0 and rep.iters < 60
+    assert hist[-1] <= 1e-10 * max(hist[0], np.abs(rhs).max())

@@ -1,0 +1,121 @@
+"""The oracle pinned against the reference's own known answers.
+
+- tests/UniaxialTension of the reference: linear displacement and constant
+  stress to 1e-8 (finite differences are exact on linear fields);
+- tests/Solid/reference/{linear,affine}-cubic.dat: trac_xhi_x(t) of the 4^3
+  cell tension test to the reference test's tolerance 1e-4 (fixture
+  tests/golden/solid_trac_xhi.json, made by tests/golden/make_golden.py);
+- src/Test/Numeric/Stencil.H:58-106: derivative accuracy below 1e-2 on
+  cos(pi x/L) cos(pi y/L) cos(pi z/L) with 32 cells.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from alamo_gb300 import bc as B
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+UNIAXIAL_BC = {
+    "type.xlo": "disp trac trac", "type.xhi": "disp trac trac", "val.xhi": "0.1 0 0",
+    "type.ylo": "trac disp trac", "type.yhi": "trac trac trac", "type.zlo": "trac trac disp",
+    "type.zhi": "trac trac trac",
+    "type.xloylo": "disp trac trac", "type.xloyhi": "disp trac trac", "type.xhiylo": "disp trac trac",
+    "type.xhiyhi": "disp trac trac", "val.xhiylo": "0.1 0 0", "val.xhiyhi": "0.1 0 0",
+    "type.zloxlo": "disp trac trac", "type.zhixlo": "disp trac trac", "type.zloxhi": "disp trac trac",
+    "type.zhixhi": "disp trac trac", "val.zloxhi": "0.1 0 0", "val.zhixhi": "0.1 0 0",
+    "type.ylozlo": "trac disp disp", "type.ylozhi": "trac disp trac", "type.yhizlo": "trac trac disp",
+    "type.yhizhi": "trac trac trac",
+    "type.xloylozlo": "disp disp disp", "type.xloylozhi": "disp disp trac", "type.xloyhizlo": "disp trac disp",
+    "type.xloyhizhi": "disp trac trac",
+    "type.xhiylozlo": "disp disp disp", "val.xhiylozlo": "0.1 0 0", "type.xhiylozhi": "disp disp trac",
+    "val.xhiylozhi": "0.1 0 0", "type.xhiyhizlo": "disp trac disp", "val.xhiyhizlo": "0.1 0 0",
+    "type.xhiyhizhi": "disp trac trac", "val.xhiyhizhi": "0.1 0 0",
+}
+
+
+def uniaxial_problem(n=33):
+    L = 16.0
+    dx = L / (n - 1)
+    E, nu = 210.0, 0.3
+    lam = E * nu / (1 + nu) / (1 - 2 * nu)
+    mu = E / 2 / (1 + nu)
+    C = np.empty((n, n, n, 2))
+    C[..., 0] = lam
+    C[..., 1] = mu
+    return C, B.Constant.parse(UNIAXIAL_BC), dx, E
+
+
+def test_uniaxial_tension_known_answer(oracle):
+    n = 33
+    C, bc, dx, E = uniaxial_problem(n)
+    bt, bv = bc.tables()
+    u0 = np.zeros((3, n, n, n))
+    b = oracle.bc_init(np.zeros_like(u0), bt, bv)
+    rhs = oracle.build_rhs(C, None, bt, u0, b, dx)
+    x, rep, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_iter=200)
+    assert rep.status == 0
+    xs = -8 + dx * np.arange(n)
+    ux = x[0, n // 2, n // 2, :]
+    exact = (xs + 8) * 0.1 / 16
+    assert np.sum((exact - ux) ** 2) / np.sum(exact ** 2) < 1e-8
+    s, _, _ = oracle.stress_strain(C, None, x, dx)
+    sig = s[n // 2, n // 2, :, 0]
+    assert np.sum((sig - E * 0.1 / 16) ** 2) / np.sum(np.full_like(sig, E * 0.1 / 16) ** 2) < 1e-8
+
+
+def _integrate(x, y):
+    return sum(0.5 * (y[i + 1] + y[i]) * (x[i + 1] - x[i]) for i in range(len(x) - 1))
+
+
+@pytest.mark.parametrize("name,f0", [("linear-cubic", None), ("affine-cubic", 0.001)])
+def test_solid_tension_series(oracle, name, f0):
+    with open(os.path.join(GOLDEN, "solid_trac_xhi.json")) as f:
+        ref = json.load(f)[name]
+    rt, rtr = np.array(ref["time"]), np.array(ref["trac_xhi_x"])
+    n, dx = 5, 0.25
+    C = np.empty((n, n, n, 21))
+    C[...] = oracle.cubic(168.3, 1.221, 0.757, np.eye(3))
+    F0 = None if f0 is None else np.full((n, n, n), f0)
+    u = np.zeros((3, n, n, n))
+    times, trac = [], []
+    for step in range(100):
+        t = 0.01 * step
+        bt, bv = B.TensionTest("uniaxial_stress", disp=0.01 * t).tables()
+        b = oracle.bc_init(np.zeros_like(u), bt, bv)
+        rhs = oracle.build_rhs(C, F0, bt, u, b, dx)
+        du, rep, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-8, tol_abs=1e-8, max_iter=30)
+        u = u + du
+        s, _, _ = oracle.stress_strain(C, F0, u, dx)
+        sxx = s[..., 0]
+        tot = 0.0
+        for k in range(n - 1):
+            for j in range(n - 1):
+                tot += 0.25 * (sxx[k, j, n - 1] + sxx[k, j + 1, n - 1] + sxx[k + 1, j, n - 1] +
+                               sxx[k + 1, j + 1, n - 1]) * dx * dx
+        times.append(t)
+        trac.append(tot)
+    times, trac = np.array(times), np.array(trac)
+    diff = np.interp(times, rt, rtr) - trac
+    err = np.sqrt(_integrate(times, diff ** 2)) / np.sqrt(_integrate(rt, rtr * rtr))
+    assert err < 1e-4, err
+
+
+@pytest.mark.parametrize("which", [100, 10, 1, 200, 20, 2, 110, 101, 11])
+def test_stencil_accuracy(oracle, which):
+    n = 33
+    Lb = 1.0
+    dx = Lb / (n - 1)
+    x = np.arange(n) * dx
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    k = np.pi / Lb
+    order = [which // 100, (which // 10) % 10, which % 10]
+    f = np.cos(k * X) * np.cos(k * Y) * np.cos(k * Z)
+    exact = np.ones_like(f) * k ** sum(order)
+    for coord, o in zip([X, Y, Z], order):
+        exact = exact * np.cos(k * coord + o * np.pi / 2)
+    d = oracle.derivative(which, f, dx)
+    s = (slice(1, -1),) * 3
+    assert np.abs(d[s] - exact[s]).max() / np.abs(exact[s]).max() < 1e-2
