@@ -15,7 +15,7 @@ EXPORTS = [
     "agb_elastic_set_stream", "agb_elastic_set_model", "agb_elastic_get_model", "agb_elastic_set_bc",
     "agb_elastic_prepare", "agb_elastic_num_levels", "agb_elastic_level_dims", "agb_elastic_fapply",
     "agb_elastic_fapply_f32", "agb_elastic_diagonal", "agb_elastic_fsmooth", "agb_elastic_residual",
-    "agb_elastic_restrict", "agb_elastic_prolong_add", "agb_elastic_bc_init", "agb_elastic_build_rhs",
+    "agb_elastic_restrict", "agb_elastic_prolong_add", "agb_elastic_vcycle", "agb_elastic_bc_init", "agb_elastic_build_rhs",
     "agb_linear_solve", "agb_newton_solve", "agb_elastic_stress_strain", "agb_profile_enable",
     "agb_profile_reset", "agb_profile_get", "agb_launch_count", "agb_cubic_stiffness", "agb_synth_uniform",
     "agb_synth_inclusion_iso", "agb_synth_voronoi_cubic", "agb_synth_spheres_iso", "agb_status_string",
@@ -26,6 +26,8 @@ AGB_OK, AGB_NOT_CONVERGED, AGB_NAN, AGB_BAD_ARG, AGB_CUDA_ERROR, AGB_NOT_READY, 
 MEM_HOST, MEM_DEVICE = 0, 1
 SYM_ISOTROPIC, SYM_MAJORMINOR = 0, 1
 PRECISION_FP64, PRECISION_MIXED = 0, 1
+SOLVER_VCYCLE, SOLVER_FGMRES = 0, 1
+BOTTOM_BICGSTAB, BOTTOM_DIRECT, BOTTOM_SMOOTHER = 0, 1, 2
 K_FAPPLY_F64, K_JACOBI_F64, K_RESIDUAL_F64, K_FAPPLY_F32, K_JACOBI_F32, K_RESIDUAL_F32, K_RESTRICT, K_PROLONG, \
     K_BOTTOM = range(9)
 
@@ -47,6 +49,11 @@ class SolverOpts(ctypes.Structure):
         ("verbose", ctypes.c_int),
         ("precision", ctypes.c_int),
         ("inner_cycles", ctypes.c_int),
+        ("solver", ctypes.c_int),
+        ("krylov_dim", ctypes.c_int),
+        ("inner_tol", ctypes.c_double),
+        ("bottom_solver", ctypes.c_int),
+        ("reserved_opts", ctypes.c_int),
     ]
 
 

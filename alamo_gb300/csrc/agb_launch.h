@@ -83,3 +83,35 @@ cudaError_t launch_bottom_bicgstab(int sym, const double* C, const double* diag,
                                    double tol_rel, double tol_abs, int* info, cudaStream_t s);
 
 }  // namespace agb
+
+namespace agb {
+// Krylov helpers (FP64 accumulation for every type)
+int multidot_blocks();
+// out[i] = <V_i, w>, i < k <= 40; part: multidot_blocks() * 40 doubles
+template <typename T>
+cudaError_t launch_multidot(const T* const* V, int k, const T* w, int64_t n, double* part, double* out,
+                            cudaStream_t s);
+// w = beta w + scale * sum_i coef[i] V_i   (coef in device memory)
+template <typename T>
+cudaError_t launch_multiaxpy(T* w, double beta, const T* const* V, const double* coef, double scale, int k, int64_t n,
+                             cudaStream_t s);
+// every elementwise helper takes (inputs, outputs, n, scale)
+// dst = a * src
+template <typename T>
+cudaError_t launch_scale_copy(const T* src, T* dst, int64_t n, double a, cudaStream_t s);
+// y(double) += a * x
+template <typename TI>
+cudaError_t launch_axpy_to_double(const TI* x, double* y, int64_t n, double a, cudaStream_t s);
+// out = a * in(double)
+template <typename TO>
+cudaError_t launch_from_double(const double* in, TO* out, int64_t n, double a, cudaStream_t s);
+}  // namespace agb
+
+namespace agb {
+// Dense direct bottom solve (nb = 3 N unknowns of the coarsest level):
+// work >= 4 nb^2 + 2 nb doubles, iwork >= 2 nb ints; flag[0] = 1 when a
+// pivot below `tiny` (the level's operator is singular to working precision).
+cudaError_t build_dense_inverse(int sym, const double* C, const LevelGeom<double>& G, const BcTable& bc,
+                                double* Ainv, double* work, int* iwork, int* flag, double tiny, cudaStream_t s);
+cudaError_t launch_dense_bottom(const double* Ainv, const double* rhs, double* sol, int nb, cudaStream_t s);
+}  // namespace agb

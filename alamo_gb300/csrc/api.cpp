@@ -64,6 +64,33 @@ struct Lev {
     T* tmp = nullptr;     // Jacobi ping-pong buffer
 };
 
+// Krylov space of the flexible GMRES: Arnoldi basis V (m+1 vectors), the
+// preconditioned directions Z (m vectors), work vector w and correction e,
+// all fine-level sized, plus device pointer tables for the fused kernels.
+template <typename T>
+struct Krylov {
+    int m = 0;
+    int64_t n = 0;
+    std::vector<T*> V, Z;
+    T** Vdev = nullptr;
+    T** Zdev = nullptr;
+    T** Wdev = nullptr;  // {w}
+    T* w = nullptr;
+    T* e = nullptr;
+    double* part = nullptr;
+    double* dots = nullptr;  // 3 * 40 device doubles
+    double* hdots = nullptr; // pinned host mirror
+    void release() {
+        for (T* p : V) cudaFree(p);
+        for (T* p : Z) cudaFree(p);
+        V.clear(); Z.clear();
+        cudaFree(Vdev); cudaFree(Zdev); cudaFree(Wdev); cudaFree(w); cudaFree(e); cudaFree(part); cudaFree(dots);
+        if (hdots) cudaFreeHost(hdots);
+        Vdev = Zdev = Wdev = nullptr; w = e = nullptr; part = dots = hdots = nullptr;
+        m = 0; n = 0;
+    }
+};
+
 }  // namespace
 
 struct agb_elastic {
@@ -90,6 +117,12 @@ struct agb_elastic {
     double* io[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t io_cap[4] = {0, 0, 0, 0};
     double* dw = nullptr;  // 9N scratch of the Newton RHS
+    Krylov<double> K64;
+    Krylov<float> K32;
+    // dense direct bottom solve
+    double* bot_inv = nullptr;
+    int bot_nb = 0;
+    bool bot_dense = false;
     // profiling
     bool prof = false;
     int64_t prof_count[AGB_K_NFAMILIES] = {0};
@@ -232,6 +265,42 @@ agb_status alloc_levels32(agb_elastic* h) {
     return AGB_OK;
 }
 
+
+// Explicit inverse of the coarsest level's operator for the direct bottom
+// solve; falls back to BiCGStab (bot_dense = false) when it is too large or
+// singular to working precision.
+agb_status build_bottom_dense(agb_elastic* h) {
+    Lev<double>& b = h->L64.back();
+    const int nb = (int)(3 * b.G.N);
+    if (nb > 4000) return AGB_OK;
+    if (h->bot_nb != nb) {
+        cudaFree(h->bot_inv);
+        h->bot_inv = nullptr;
+        CK(cudaMalloc(&h->bot_inv, sizeof(double) * (size_t)nb * nb));
+        h->bot_nb = nb;
+    }
+    double* work = nullptr;
+    int* iwork = nullptr;
+    CK(cudaMallocAsync((void**)&work, sizeof(double) * (4 * (size_t)nb * nb + 2 * (size_t)nb), h->stream));
+    CK(cudaMallocAsync((void**)&iwork, sizeof(int) * (2 * (size_t)nb + 1), h->stream));
+    // pivot threshold relative to the largest diagonal entry of the level
+    std::vector<double> dg(nb);
+    CK(cudaMemcpyAsync(dg.data(), b.diag, sizeof(double) * nb, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    double dmax = 0.0;
+    for (double v : dg) dmax = std::max(dmax, std::fabs(v));
+    int* flag = iwork + 2 * nb;
+    CK(build_dense_inverse(h->sym, b.C, b.G, h->bc, h->bot_inv, work, iwork, flag, 1e-12 * dmax, h->stream));
+    h->launches += 2 * nb + 3;
+    int hflag = 0;
+    CK(cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaFreeAsync(work, h->stream));
+    CK(cudaFreeAsync(iwork, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->bot_dense = (hflag == 0);
+    return AGB_OK;
+}
+
 // ---------------------------------------------------------------- prepare
 agb_status prepare(agb_elastic* h) {
     if (h->prepared) return AGB_OK;
@@ -245,6 +314,8 @@ agb_status prepare(agb_elastic* h) {
         CK(launch_diagonal<double>(h->sym, h->L64[l].C, h->L64[l].G, h->bc, h->L64[l].diag, h->stream));
         h->launches++;
     }
+    h->bot_dense = false;
+    if (h->opts.bottom_solver == AGB_BOTTOM_DIRECT) TRY(build_bottom_dense(h));
     if (h->opts.precision == AGB_PRECISION_MIXED) {
         if (h->L32.size() != h->L64.size()) TRY(alloc_levels32(h));
         for (int l = 0; l < nl; l++) {
@@ -305,10 +376,18 @@ agb_status smooth(agb_elastic* h, std::vector<Lev<T>>& L, int l, int ncalls, boo
 }
 
 agb_status bottom64(agb_elastic* h, Lev<double>& b) {
-    CK(cudaMemsetAsync(b.cor, 0, sizeof(double) * 3 * b.G.N, h->stream));
     ProfScope ps(h, AGB_K_BOTTOM, true);
+    if (h->opts.bottom_solver == AGB_BOTTOM_DIRECT && h->bot_dense) {
+        CK(launch_dense_bottom(h->bot_inv, b.res, b.cor, h->bot_nb, h->stream));
+        h->launches++;
+        return AGB_OK;
+    }
+    CK(cudaMemsetAsync(b.cor, 0, sizeof(double) * 3 * b.G.N, h->stream));
+    // the smoother as bottom solver: no BiCGStab iteration, straight to the
+    // zeroed correction and final_smooth Fsmooth calls
+    const int bmax = h->opts.bottom_solver == AGB_BOTTOM_SMOOTHER ? 0 : h->opts.bottom_max_iter;
     CK(launch_bottom_bicgstab_ex(h->sym, b.C, b.diag, b.G, h->bc, b.res, b.cor, h->bottom_work,
-                                 h->opts.bottom_max_iter, h->opts.bottom_tol_rel, h->opts.bottom_tol_abs,
+                                 bmax, h->opts.bottom_tol_rel, h->opts.bottom_tol_abs,
                                  h->opts.bottom_smooth, h->opts.final_smooth, h->opts.omega, h->bottom_info,
                                  h->stream));
     h->launches++;
@@ -392,6 +471,129 @@ agb_status vec_norms(agb_elastic* h, const double* v, int64_t n, double out[2]) 
     return AGB_OK;
 }
 
+
+template <typename T>
+Krylov<T>& krylov_of(agb_elastic* h);
+template <>
+Krylov<double>& krylov_of<double>(agb_elastic* h) { return h->K64; }
+template <>
+Krylov<float>& krylov_of<float>(agb_elastic* h) { return h->K32; }
+
+template <typename T>
+agb_status ensure_krylov(agb_elastic* h, int m, int64_t n) {
+    Krylov<T>& K = krylov_of<T>(h);
+    if (K.m >= m && K.n == n) return AGB_OK;
+    K.release();
+    K.V.assign(m + 1, nullptr);
+    K.Z.assign(m, nullptr);
+    for (int i = 0; i <= m; i++) CK(cudaMalloc(&K.V[i], sizeof(T) * n));
+    for (int i = 0; i < m; i++) CK(cudaMalloc(&K.Z[i], sizeof(T) * n));
+    CK(cudaMalloc(&K.w, sizeof(T) * n));
+    CK(cudaMalloc(&K.e, sizeof(T) * n));
+    CK(cudaMalloc(&K.Vdev, sizeof(T*) * (m + 1)));
+    CK(cudaMalloc(&K.Zdev, sizeof(T*) * m));
+    CK(cudaMalloc(&K.Wdev, sizeof(T*)));
+    CK(cudaMalloc(&K.part, sizeof(double) * multidot_blocks() * 40));
+    CK(cudaMalloc(&K.dots, sizeof(double) * 3 * 40));
+    CK(cudaMallocHost(&K.hdots, sizeof(double) * 3 * 40));
+    CK(cudaMemcpy(K.Vdev, K.V.data(), sizeof(T*) * (m + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(K.Zdev, K.Z.data(), sizeof(T*) * m, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(K.Wdev, &K.w, sizeof(T*), cudaMemcpyHostToDevice));
+    K.m = m;
+    K.n = n;
+    return AGB_OK;
+}
+
+// One cycle of flexible GMRES (Saad 1993) on A e = r for the fine level of
+// the hierarchy L, right-preconditioned by one V-cycle, classical
+// Gram-Schmidt with one re-orthogonalisation; stops when the Arnoldi
+// residual estimate falls below rel_tol * ||r||_2 or after m steps.
+// Result in K.e; its = V-cycles applied; est = estimated relative residual.
+template <typename T>
+agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, double rel_tol, int maxit, int* its,
+                        double* est) {
+    Lev<T>& top = L[0];
+    const int64_t n = 3 * top.G.N;
+    const int m = std::min(h->opts.krylov_dim, std::max(1, maxit));
+    TRY(ensure_krylov<T>(h, h->opts.krylov_dim, n));
+    Krylov<T>& K = krylov_of<T>(h);
+    cudaStream_t st = h->stream;
+    // beta = ||r||_2
+    CK(cudaMemcpyAsync(K.w, r, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
+    CK(launch_multidot<T>(K.Wdev, 1, K.w, n, K.part, K.dots, st));
+    CK(cudaMemcpyAsync(K.hdots, K.dots, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    h->launches += 2;
+    const double beta = std::sqrt(K.hdots[0]);
+    *its = 0;
+    *est = 0.0;
+    if (!(beta > 0.0)) {
+        CK(cudaMemsetAsync(K.e, 0, sizeof(T) * n, st));
+        return AGB_OK;
+    }
+    CK(launch_scale_copy<T>(r, K.V[0], n, 1.0 / beta, st));
+    h->launches++;
+    std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m, 0.0), sn(m, 0.0), g(m + 1, 0.0);
+    g[0] = beta;
+    int j = 0;
+    double resid = beta;
+    for (; j < m; j++) {
+        // Z_j = M^-1 V_j (one V-cycle on the correction equation)
+        CK(cudaMemcpyAsync(top.res, K.V[j], sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
+        TRY(vcycle<T>(h, L));
+        CK(cudaMemcpyAsync(K.Z[j], top.cor, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
+        // w = A Z_j
+        CK(launch_fapply<T>(h->sym, K.Z[j], top.C, top.G, h->bc, K.w, st));
+        // CGS2
+        CK(launch_multidot<T>(K.Vdev, j + 1, K.w, n, K.part, K.dots, st));
+        CK(launch_multiaxpy<T>(K.w, 1.0, K.Vdev, K.dots, -1.0, j + 1, n, st));
+        CK(launch_multidot<T>(K.Vdev, j + 1, K.w, n, K.part, K.dots + 40, st));
+        CK(launch_multiaxpy<T>(K.w, 1.0, K.Vdev, K.dots + 40, -1.0, j + 1, n, st));
+        CK(launch_multidot<T>(K.Wdev, 1, K.w, n, K.part, K.dots + 80, st));
+        CK(cudaMemcpyAsync(K.hdots, K.dots, sizeof(double) * 120, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        h->launches += 12;
+        for (int i = 0; i <= j; i++) H[(size_t)i * m + j] = K.hdots[i] + K.hdots[40 + i];
+        const double hn = std::sqrt(std::max(K.hdots[80], 0.0));
+        H[(size_t)(j + 1) * m + j] = hn;
+        if (hn > 0.0) {
+            CK(launch_scale_copy<T>(K.w, K.V[j + 1], n, 1.0 / hn, st));
+            h->launches++;
+        }
+        // Givens rotations on column j
+        for (int i = 0; i < j; i++) {
+            const double a = H[(size_t)i * m + j], b = H[(size_t)(i + 1) * m + j];
+            H[(size_t)i * m + j] = cs[i] * a + sn[i] * b;
+            H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * b;
+        }
+        const double a = H[(size_t)j * m + j], b = H[(size_t)(j + 1) * m + j];
+        const double rr = std::hypot(a, b);
+        cs[j] = rr > 0 ? a / rr : 1.0;
+        sn[j] = rr > 0 ? b / rr : 0.0;
+        H[(size_t)j * m + j] = rr;
+        H[(size_t)(j + 1) * m + j] = 0.0;
+        g[j + 1] = -sn[j] * g[j];
+        g[j] = cs[j] * g[j];
+        resid = std::fabs(g[j + 1]);
+        if (resid <= rel_tol * beta || !(hn > 0.0)) { j++; break; }
+    }
+    const int k = std::min(j, m);
+    // y = H^-1 g (upper triangular k x k), e = Z y
+    std::vector<double> y(k, 0.0);
+    for (int i = k - 1; i >= 0; i--) {
+        double t = g[i];
+        for (int q = i + 1; q < k; q++) t -= H[(size_t)i * m + q] * y[q];
+        y[i] = H[(size_t)i * m + i] != 0.0 ? t / H[(size_t)i * m + i] : 0.0;
+    }
+    std::memcpy(K.hdots, y.data(), sizeof(double) * k);
+    CK(cudaMemcpyAsync(K.dots, K.hdots, sizeof(double) * k, cudaMemcpyHostToDevice, st));
+    CK(launch_multiaxpy<T>(K.e, 0.0, K.Zdev, K.dots, 1.0, k, n, st));
+    h->launches++;
+    *its = k;
+    *est = resid / beta;
+    return AGB_OK;
+}
+
 // Linear::solve on device pointers.
 agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_rel, double tol_abs,
                      agb_solve_report* rep) {
@@ -415,7 +617,26 @@ agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_re
     else if (r[0] <= target && !fixed) status = AGB_OK;
     else {
         while (it < maxit) {
-            if (!mixed) {
+            if (h->opts.solver == AGB_SOLVER_FGMRES) {
+                int its = 0;
+                double est = 0.0;
+                if (mixed) {
+                    // FP32 FGMRES(V-cycle) on the scaled FP64 residual, FP64 update
+                    const double s = (r[0] > 0.0) ? 1.0 / r[0] : 1.0;
+                    Lev<float>& t32 = h->L32[0];
+                    CK(launch_from_double<float>(top.res, t32.rescor, n3, s, h->stream));
+                    h->launches++;
+                    TRY(fgmres_cycle<float>(h, h->L32, t32.rescor, h->opts.inner_tol, maxit - it, &its, &est));
+                    CK(launch_axpy_to_double<float>(h->K32.e, x, n3, 1.0 / s, h->stream));
+                } else {
+                    // FP64 FGMRES(V-cycle); aim a little below the target, the true residual decides
+                    const double rt = std::max(0.5 * target / std::max(r[0], 1e-300), 1e-15);
+                    TRY(fgmres_cycle<double>(h, h->L64, top.res, std::min(rt, 0.5), maxit - it, &its, &est));
+                    CK(launch_axpy_to_double<double>(h->K64.e, x, n3, 1.0, h->stream));
+                }
+                h->launches++;
+                it += std::max(its, 1);
+            } else if (!mixed) {
                 TRY(vcycle<double>(h, h->L64));
                 CK(launch_axpy(1.0, top.cor, x, n3, h->stream));
                 h->launches++;
@@ -524,6 +745,11 @@ agb_status agb_default_opts(agb_solver_opts* o) {
     o->verbose = 0;
     o->precision = AGB_PRECISION_FP64;
     o->inner_cycles = 1;
+    o->solver = AGB_SOLVER_VCYCLE;
+    o->krylov_dim = 20;
+    o->inner_tol = 1e-4;
+    o->bottom_solver = AGB_BOTTOM_BICGSTAB;
+    o->reserved_opts = 0;
     return AGB_OK;
 }
 
@@ -534,6 +760,13 @@ static agb_status check_opts(const agb_solver_opts* o) {
     if (!(o->omega > 0.0) || !(o->omega <= 2.0)) return fail(AGB_BAD_ARG, "omega must lie in (0, 2]");
     if (o->precision != AGB_PRECISION_FP64 && o->precision != AGB_PRECISION_MIXED)
         return fail(AGB_BAD_ARG, "unknown precision");
+    if (o->solver != AGB_SOLVER_VCYCLE && o->solver != AGB_SOLVER_FGMRES) return fail(AGB_BAD_ARG, "unknown solver");
+    if (o->bottom_solver < AGB_BOTTOM_BICGSTAB || o->bottom_solver > AGB_BOTTOM_SMOOTHER)
+        return fail(AGB_BAD_ARG, "unknown bottom solver");
+    if (o->solver == AGB_SOLVER_FGMRES && (o->krylov_dim < 1 || o->krylov_dim > 39))
+        return fail(AGB_BAD_ARG, "krylov_dim must lie in [1, 39]");
+    if (o->solver == AGB_SOLVER_FGMRES && !(o->inner_tol > 0.0 && o->inner_tol < 1.0))
+        return fail(AGB_BAD_ARG, "inner_tol must lie in (0, 1)");
     return AGB_OK;
 }
 
@@ -587,6 +820,9 @@ agb_status agb_elastic_destroy(agb_elastic* h) {
     cudaFree(h->bottom_info);
     cudaFree(h->bcval_dev);
     cudaFree(h->dw);
+    h->K64.release();
+    h->K32.release();
+    cudaFree(h->bot_inv);
     for (int s = 0; s < 4; s++) cudaFree(h->io[s]);
     for (auto e : h->ev_pool) cudaEventDestroy(e);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -826,6 +1062,36 @@ agb_status agb_elastic_prolong_add(agb_elastic* h, int fine_level, const double*
     CK(launch_prolong_add<double>((const double*)dc, c.G, (double*)df0, f.G, h->stream));
     h->launches++;
     return finish_out(h, fine, df0, fb, where);
+}
+
+agb_status agb_elastic_vcycle(agb_elastic* h, const double* res, double* cor, int precision, int where) {
+    TRY(check_level(h, 0));
+    TRY(prepare(h));
+    if (!res || !cor) return fail(AGB_BAD_ARG, "null argument");
+    if (precision != AGB_PRECISION_FP64 && precision != AGB_PRECISION_MIXED) return fail(AGB_BAD_ARG, "bad precision");
+    Lev<double>& top = h->L64[0];
+    const int64_t n3 = 3 * top.G.N;
+    const size_t bytes = sizeof(double) * n3;
+    const void* dr = nullptr;
+    void* dc = nullptr;
+    TRY(dev_in(h, 0, res, bytes, where, &dr));
+    TRY(dev_out(h, 1, cor, bytes, where, &dc));
+    if (precision == AGB_PRECISION_FP64) {
+        CK(cudaMemcpyAsync(top.res, dr, bytes, cudaMemcpyDeviceToDevice, h->stream));
+        TRY(vcycle<double>(h, h->L64));
+        CK(cudaMemcpyAsync(dc, top.cor, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    } else {
+        TRY(ensure_f32(h));
+        Lev<float>& t32 = h->L32[0];
+        CK(launch_from_double<float>((const double*)dr, t32.res, n3, 1.0, h->stream));
+        TRY(vcycle<float>(h, h->L32));
+        CK(cudaMemsetAsync(dc, 0, bytes, h->stream));
+        CK(launch_axpy_to_double<float>(t32.cor, (double*)dc, n3, 1.0, h->stream));
+        h->launches += 2;
+    }
+    TRY(finish_out(h, cor, dc, bytes, where));
+    prof_collect(h);
+    return AGB_OK;
 }
 
 agb_status agb_elastic_bc_init(agb_elastic* h, double* b, int homogeneous, int where) {

@@ -204,3 +204,154 @@ cudaError_t launch_bottom_bicgstab(int sym, const double* C, const double* diag,
 }
 
 }  // namespace agb
+
+namespace agb {
+
+// ---------------------------------------------------------------------------
+// Direct bottom solve: the coarsest level's operator is assembled as a dense
+// matrix (column j = A e_j, probing the same per-node arithmetic as Fapply),
+// inverted once per prepareForSolve by Gauss-Jordan elimination with partial
+// pivoting, and every bottom solve is then one dense matrix-vector product.
+// ---------------------------------------------------------------------------
+
+// Acol[j * nb + i] = (A e_j)_i ; E is nb*nb scratch holding the unit vectors
+template <int SYM>
+__global__ void __launch_bounds__(256) k_assemble(const double* __restrict__ C, LevelGeom<double> G, BcTable bc,
+                                                  double* __restrict__ E, double* __restrict__ Acol, int nb) {
+    const int j = blockIdx.y;
+    double* u = E + (int64_t)j * nb;
+    // every block builds its own unit vector, then applies the operator
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) u[q] = (q == j) ? 1.0 : 0.0;
+    __syncthreads();
+    for (int64_t node = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; node < G.N;
+         node += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(node / G.sz);
+        const int64_t rem = node - (int64_t)k * G.sz;
+        const int jj = (int)(rem / G.nx);
+        const int i = (int)(rem - (int64_t)jj * G.nx);
+        double f[3];
+        apply_node<double, SYM>(u, C, G, bc, i, jj, k, node, f);
+        for (int c = 0; c < 3; c++) Acol[(int64_t)j * nb + c * G.N + node] = f[c];
+    }
+}
+
+// W = [A | I], row-major nb x 2nb, from the column-major probe result
+__global__ void k_gj_init(const double* __restrict__ Acol, double* __restrict__ W, int nb, int* __restrict__ used) {
+    const int64_t tot = (int64_t)nb * 2 * nb;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(q / (2 * nb)), c = (int)(q - (int64_t)r * 2 * nb);
+        W[q] = (c < nb) ? Acol[(int64_t)c * nb + r] : ((c - nb) == r ? 1.0 : 0.0);
+    }
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nb; r += gridDim.x * blockDim.x) used[r] = 0;
+}
+
+// pivot of column k among the rows not used yet; prow = pivot row / pivot
+__global__ void __launch_bounds__(1024) k_gj_pivot(double* __restrict__ W, int nb, int k, int* __restrict__ used,
+                                                   int* __restrict__ perm, double* __restrict__ prow,
+                                                   int* __restrict__ flag, double tiny) {
+    __shared__ double bv[32];
+    __shared__ int bi[32];
+    double best = -1.0;
+    int bidx = -1;
+    for (int r = threadIdx.x; r < nb; r += blockDim.x) {
+        if (used[r]) continue;
+        const double a = fabs(W[(int64_t)r * 2 * nb + k]);
+        if (a > best) { best = a; bidx = r; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+        if (ob > best || (ob == best && oi >= 0 && (bidx < 0 || oi < bidx))) { best = ob; bidx = oi; }
+    }
+    if ((threadIdx.x & 31) == 0) { bv[threadIdx.x >> 5] = best; bi[threadIdx.x >> 5] = bidx; }
+    __syncthreads();
+    __shared__ int p_sh;
+    __shared__ double piv_sh;
+    if (threadIdx.x == 0) {
+        double b = -1.0;
+        int p = -1;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++)
+            if (bv[w] > b || (bv[w] == b && bi[w] >= 0 && (p < 0 || bi[w] < p))) { b = bv[w]; p = bi[w]; }
+        if (p < 0 || !(b > tiny)) { flag[0] = 1; p = (p < 0) ? 0 : p; }
+        used[p] = 1;
+        perm[k] = p;
+        p_sh = p;
+        piv_sh = W[(int64_t)p * 2 * nb + k];
+    }
+    __syncthreads();
+    const int p = p_sh;
+    const double inv = (piv_sh != 0.0) ? 1.0 / piv_sh : 0.0;
+    for (int c = threadIdx.x; c < 2 * nb; c += blockDim.x) prow[c] = W[(int64_t)p * 2 * nb + c] * inv;
+}
+
+// eliminate column k from every row but the pivot row, which becomes prow
+__global__ void __launch_bounds__(256) k_gj_elim(double* __restrict__ W, int nb, int k, const int* __restrict__ perm,
+                                                 const double* __restrict__ prow) {
+    const int p = perm[k];
+    for (int r = blockIdx.x; r < nb; r += gridDim.x) {
+        double* row = W + (int64_t)r * 2 * nb;
+        if (r == p) {
+            for (int c = threadIdx.x; c < 2 * nb; c += blockDim.x) row[c] = prow[c];
+        } else {
+            const double f = row[k];
+            __syncthreads();
+            if (f != 0.0)
+                for (int c = threadIdx.x; c < 2 * nb; c += blockDim.x) row[c] -= f * prow[c];
+        }
+        __syncthreads();
+    }
+}
+
+// Ainv[k][j] = W[perm[k]][nb + j]
+__global__ void k_gj_extract(const double* __restrict__ W, const int* __restrict__ perm, double* __restrict__ Ainv,
+                             int nb) {
+    const int64_t tot = (int64_t)nb * nb;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(q / nb), j = (int)(q - (int64_t)k * nb);
+        Ainv[q] = W[(int64_t)perm[k] * 2 * nb + nb + j];
+    }
+}
+
+cudaError_t build_dense_inverse(int sym, const double* C, const LevelGeom<double>& G, const BcTable& bc,
+                                double* Ainv, double* work, int* iwork, int* flag, double tiny, cudaStream_t s) {
+    const int nb = (int)(3 * G.N);
+    double* E = work;                          // nb*nb
+    double* Acol = work + (int64_t)nb * nb;    // nb*nb
+    double* W = work + 2 * (int64_t)nb * nb;   // 2*nb*nb
+    double* prow = work + 4 * (int64_t)nb * nb;// 2*nb
+    int* used = iwork;
+    int* perm = iwork + nb;
+    dim3 grd((unsigned)((G.N + 255) / 256), (unsigned)nb);
+    if (sym == SYM_ISO) k_assemble<SYM_ISO><<<grd, 256, 0, s>>>(C, G, bc, E, Acol, nb);
+    else k_assemble<SYM_MM><<<grd, 256, 0, s>>>(C, G, bc, E, Acol, nb);
+    k_gj_init<<<152 * 4, 256, 0, s>>>(Acol, W, nb, used);
+    cudaMemsetAsync(flag, 0, sizeof(int), s);
+    const int eb = nb < 152 * 8 ? nb : 152 * 8;
+    for (int k = 0; k < nb; k++) {
+        k_gj_pivot<<<1, 1024, 0, s>>>(W, nb, k, used, perm, prow, flag, tiny);
+        k_gj_elim<<<eb, 256, 0, s>>>(W, nb, k, perm, prow);
+    }
+    k_gj_extract<<<152 * 4, 256, 0, s>>>(W, perm, Ainv, nb);
+    return cudaGetLastError();
+}
+
+// sol = Ainv * rhs, one warp per row
+__global__ void __launch_bounds__(256) k_dense_matvec(const double* __restrict__ Ainv, const double* __restrict__ b,
+                                                      double* __restrict__ x, int nb) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= nb) return;
+    const double* row = Ainv + (int64_t)warp * nb;
+    double acc = 0.0;
+    for (int j = lane; j < nb; j += 32) acc += row[j] * b[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) x[warp] = acc;
+}
+
+cudaError_t launch_dense_bottom(const double* Ainv, const double* rhs, double* sol, int nb, cudaStream_t s) {
+    k_dense_matvec<<<(nb * 32 + 255) / 256, 256, 0, s>>>(Ainv, rhs, sol, nb);
+    return cudaGetLastError();
+}
+
+}  // namespace agb

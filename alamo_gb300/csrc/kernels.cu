@@ -564,3 +564,139 @@ cudaError_t launch_stress_strain(int sym, const double* u, const double* F0, int
 }
 
 }  // namespace agb
+
+namespace agb {
+
+// ---------------------------------------------------------------- Krylov
+// out[i] = sum_q V_i[q] * w[q] for i < k (FP64 accumulation), two passes:
+// per-block partial sums, then one block per i over the partials.
+static constexpr int KMAX = 40;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_multidot_partial(const T* const* __restrict__ V, int k, const T* __restrict__ w,
+                                                          int64_t n, double* __restrict__ part) {
+    double acc[KMAX];
+#pragma unroll
+    for (int i = 0; i < KMAX; i++) acc[i] = 0.0;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const double wq = (double)w[q];
+#pragma unroll 4
+        for (int i = 0; i < k; i++) acc[i] += (double)V[i][q] * wq;
+    }
+    __shared__ double sh[8][KMAX];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i = 0; i < k; i++) {
+        double v = acc[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[wid][i] = v;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+        double s = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += sh[q][i];
+        part[(int64_t)blockIdx.x * KMAX + i] = s;
+    }
+}
+
+__global__ void k_multidot_final(const double* __restrict__ part, int nb, int k, double* __restrict__ out) {
+    const int i = blockIdx.x;
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += part[(int64_t)b * KMAX + i];
+    __shared__ double sh[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[q];
+        out[i] = t;
+    }
+}
+
+int multidot_blocks() { return 152 * 4; }
+
+template <typename T>
+cudaError_t launch_multidot(const T* const* V, int k, const T* w, int64_t n, double* part, double* out,
+                            cudaStream_t s) {
+    if (k < 1 || k > KMAX) return cudaErrorInvalidValue;
+    const int nb = multidot_blocks();
+    k_multidot_partial<T><<<nb, 256, 0, s>>>(V, k, w, n, part);
+    k_multidot_final<<<k, 256, 0, s>>>(part, nb, k, out);
+    return cudaGetLastError();
+}
+template cudaError_t launch_multidot<double>(const double* const*, int, const double*, int64_t, double*, double*,
+                                             cudaStream_t);
+template cudaError_t launch_multidot<float>(const float* const*, int, const float*, int64_t, double*, double*,
+                                            cudaStream_t);
+
+// w = beta * w + sum_i coef[i] * scale * V_i  (coef in device memory)
+template <typename T>
+__global__ void __launch_bounds__(256) k_multiaxpy(T* __restrict__ w, double beta, const T* const* __restrict__ V,
+                                                   const double* __restrict__ coef, double scale, int k, int64_t n) {
+    __shared__ double c[KMAX];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) c[i] = coef[i] * scale;
+    __syncthreads();
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        double acc = (beta == 0.0) ? 0.0 : beta * (double)w[q];
+        for (int i = 0; i < k; i++) acc += c[i] * (double)V[i][q];
+        w[q] = (T)acc;
+    }
+}
+
+template <typename T>
+cudaError_t launch_multiaxpy(T* w, double beta, const T* const* V, const double* coef, double scale, int k, int64_t n,
+                             cudaStream_t s) {
+    if (k < 0 || k > KMAX) return cudaErrorInvalidValue;
+    k_multiaxpy<T><<<flat_blocks(n), 256, 0, s>>>(w, beta, V, coef, scale, k, n);
+    return cudaGetLastError();
+}
+template cudaError_t launch_multiaxpy<double>(double*, double, const double* const*, const double*, double, int,
+                                              int64_t, cudaStream_t);
+template cudaError_t launch_multiaxpy<float>(float*, double, const float* const*, const double*, double, int, int64_t,
+                                             cudaStream_t);
+
+// dst = a * src
+template <typename T>
+__global__ void k_scale_copy(const T* __restrict__ src, T* __restrict__ dst, double a, int64_t n) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        dst[q] = (T)(a * (double)src[q]);
+}
+template <typename T>
+cudaError_t launch_scale_copy(const T* src, T* dst, int64_t n, double a, cudaStream_t s) {
+    k_scale_copy<T><<<flat_blocks(n), 256, 0, s>>>(src, dst, a, n);
+    return cudaGetLastError();
+}
+template cudaError_t launch_scale_copy<double>(const double*, double*, int64_t, double, cudaStream_t);
+template cudaError_t launch_scale_copy<float>(const float*, float*, int64_t, double, cudaStream_t);
+
+// out(double) = scale * in(double or float) added with weight: y += a * x (mixed types)
+template <typename TI>
+__global__ void k_axpy_to_double(const TI* __restrict__ x, double* __restrict__ y, double a, int64_t n) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        y[q] += a * (double)x[q];
+}
+template <typename TI>
+cudaError_t launch_axpy_to_double(const TI* x, double* y, int64_t n, double a, cudaStream_t s) {
+    k_axpy_to_double<TI><<<flat_blocks(n), 256, 0, s>>>(x, y, a, n);
+    return cudaGetLastError();
+}
+template cudaError_t launch_axpy_to_double<double>(const double*, double*, int64_t, double, cudaStream_t);
+template cudaError_t launch_axpy_to_double<float>(const float*, double*, int64_t, double, cudaStream_t);
+
+// out(T) = scale * in(double)
+template <typename TO>
+__global__ void k_from_double(const double* __restrict__ in, TO* __restrict__ out, double a, int64_t n) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        out[q] = (TO)(a * in[q]);
+}
+template <typename TO>
+cudaError_t launch_from_double(const double* in, TO* out, int64_t n, double a, cudaStream_t s) {
+    k_from_double<TO><<<flat_blocks(n), 256, 0, s>>>(in, out, a, n);
+    return cudaGetLastError();
+}
+template cudaError_t launch_from_double<double>(const double*, double*, int64_t, double, cudaStream_t);
+template cudaError_t launch_from_double<float>(const double*, float*, int64_t, double, cudaStream_t);
+
+}  // namespace agb

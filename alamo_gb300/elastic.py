@@ -51,6 +51,10 @@ def default_opts(**kw):
     for k, v in kw.items():
         if k == "precision" and isinstance(v, str):
             v = {"fp64": L.PRECISION_FP64, "mixed": L.PRECISION_MIXED}[v]
+        if k == "solver" and isinstance(v, str):
+            v = {"vcycle": L.SOLVER_VCYCLE, "fgmres": L.SOLVER_FGMRES}[v]
+        if k == "bottom_solver" and isinstance(v, str):
+            v = {"bicgstab": L.BOTTOM_BICGSTAB, "direct": L.BOTTOM_DIRECT, "smoother": L.BOTTOM_SMOOTHER}[v]
         setattr(o, k, v)
     return o
 
@@ -189,6 +193,17 @@ class Elastic:
         pf, wf = _arg(fine)
         L.check(L.lib().agb_elastic_prolong_add(self.h, int(fine_level), pc, pf, _same_where(wc, wf)))
         return fine
+
+    def vcycle(self, res, cor=None, precision="fp64"):
+        """One multigrid V-cycle on A cor = res from cor = 0 (MLMG::mgVcycle)."""
+        if cor is None:
+            cor = np.empty(self._vec_shape(0))
+        pr, wr = _arg(res)
+        pc, wc = _arg(cor)
+        prec = {"fp64": L.PRECISION_FP64, "mixed": L.PRECISION_MIXED, "fp32": L.PRECISION_MIXED}.get(precision,
+                                                                                                      precision)
+        L.check(L.lib().agb_elastic_vcycle(self.h, pr, pc, int(prec), _same_where(wr, wc)))
+        return cor
 
     # --- BC / RHS / post-processing -------------------------------------
     def bc_init(self, b=None, homogeneous=False):

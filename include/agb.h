@@ -54,6 +54,18 @@ typedef enum {
     AGB_BC_NONE = 4
 } agb_bc_type;
 typedef enum { AGB_PRECISION_FP64 = 0, AGB_PRECISION_MIXED = 1 } agb_precision;
+/* AGB_SOLVER_VCYCLE: V-cycles on the correction equation as amrex::MLMG runs
+ * them for the reference.  AGB_SOLVER_FGMRES: flexible GMRES whose
+ * preconditioner is one V-cycle (AMReX's GMRES-with-MLMG-preconditioner
+ * scheme); in mixed precision the FGMRES and its V-cycle run in FP32 inside
+ * FP64 iterative refinement.  Both stop on the same FP64 residual test. */
+typedef enum { AGB_SOLVER_VCYCLE = 0, AGB_SOLVER_FGMRES = 1 } agb_solver;
+/* solver.bottom_solver of the reference (Linear.H:279-281): BiCGStab (the
+ * reference's default), the smoother alone (final_smooth calls), or a dense
+ * direct solve (explicit inverse of the coarsest operator, FP64; falls back
+ * to BiCGStab when that operator is singular to working precision or has
+ * more than 4000 unknowns). */
+typedef enum { AGB_BOTTOM_BICGSTAB = 0, AGB_BOTTOM_DIRECT = 1, AGB_BOTTOM_SMOOTHER = 2 } agb_bottom_solver;
 
 /* Solver settings; field names follow the reference's `solver.*` keys
  * (Solver::Nonlocal::Linear::Parse, src/Solver/Nonlocal/Linear.H:296-382). */
@@ -71,7 +83,12 @@ typedef struct agb_solver_opts {
     int fixed_iter;           /* > 0: run exactly this many cycles */
     int verbose;
     int precision;            /* agb_precision (AGB_PRECISION_FP64) */
-    int inner_cycles;         /* mixed: FP32 V-cycles per FP64 residual (1) */
+    int inner_cycles;         /* mixed V-cycle iteration: FP32 V-cycles per FP64 residual (1) */
+    int solver;               /* agb_solver: V-cycle iteration (MLMG) or FGMRES(V-cycle) */
+    int krylov_dim;           /* FGMRES: basis size per cycle, <= 39 (20) */
+    double inner_tol;         /* mixed FGMRES: residual reduction of one FP32 inner solve (1e-4) */
+    int bottom_solver;        /* agb_bottom_solver (AGB_BOTTOM_BICGSTAB) */
+    int reserved_opts;
 } agb_solver_opts;
 
 typedef struct agb_solve_report {
@@ -146,6 +163,13 @@ agb_status agb_elastic_restrict(agb_elastic* h, int crse_level, const double* fi
 /* Operator<Grid::Node>::interpolation (src/Operator/Operator.cpp:365-434):
  * fine (level fine_level) += P crse (level fine_level+1) */
 agb_status agb_elastic_prolong_add(agb_elastic* h, int fine_level, const double* crse, double* fine, int where);
+
+/* MLMG::mgVcycle on the fine level as the reference's hooks drive it: one
+ * V-cycle on A cor = res from cor = 0 (pre-smoothing, correction residual,
+ * restriction down to the bottom solve, prolongation and post-smoothing up).
+ * precision AGB_PRECISION_MIXED runs the cycle in FP32 (res is rounded to
+ * FP32, the bottom solve stays FP64); res and cor are FP64 arrays (3*N). */
+agb_status agb_elastic_vcycle(agb_elastic* h, const double* res, double* cor, int precision, int where);
 
 /* ------------------------------------------------------------- solves */
 /* BC::Operator::Elastic::Constant::Init (src/BC/Operator/Elastic/

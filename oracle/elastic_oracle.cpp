@@ -237,6 +237,10 @@ inline void bc_row(const int* bc_type, int reg, const double nrm[3], const doubl
     }
 }
 
+// When false, interior rows drop the sum_q (d_q C : grad u)_{:,q} term (the
+// reference's m_uniform = true branch, Elastic.cpp:245).
+bool g_grad_c = true;
+
 // ---------------------------------------------------------------------------
 // Fapply at one node (Elastic.cpp:165-290; psi not set, m_uniform false)
 // ---------------------------------------------------------------------------
@@ -276,6 +280,7 @@ void fapply_node(int sym, const Grid& g, const double* C, const int* bct, const 
         b[p][2][1] = b[p][1][2];
     }
     c_hess(sym, c, b, f);
+    if (!g_grad_c) return;
     // + sum_q (d_q C * gradu)_{:,q}: central differences of C (Elastic.cpp:245-254)
     double col[3][3];
     for (int q = 0; q < 3; q++) {
@@ -492,6 +497,7 @@ struct orc_opts {
     int max_coarsening_level;  // -1 = as deep as possible
     int fixed_iter;            // -1 = run to tolerance
     int verbose;
+    int bottom_solver;         // 0 BiCGStab, 1 dense direct (exact), 2 smoother only
 };
 
 struct orc_report {
@@ -510,6 +516,10 @@ static Grid mkgrid(int nx, int ny, int nz, const double* dx) {
     g.dx[0] = dx[0]; g.dx[1] = dx[1]; g.dx[2] = dx[2];
     return g;
 }
+
+// SetUniform (src/Operator/Elastic.H:104-107): uniform = 1 drops the
+// grad-C term of interior rows.
+void orc_set_uniform(int uniform) { g_grad_c = uniform == 0; }
 
 int orc_num_threads(void) {
 #ifdef _OPENMP
@@ -839,10 +849,70 @@ struct Hier {
         return ret;
     }
 
+    // dense matrix of the coarsest operator, factorised once (Gaussian
+    // elimination with partial pivoting); empty when singular
+    std::vector<double> LU;
+    std::vector<int> piv;
+    bool dense_ok = false, dense_tried = false;
+
+    void build_dense() {
+        dense_tried = true;
+        Level& v = L.back();
+        const int nb = (int)(3 * v.g.N());
+        if (nb > 4000) return;
+        LU.assign((size_t)nb * nb, 0.0);
+        std::vector<double> e(nb, 0.0), col(nb);
+        for (int j = 0; j < nb; j++) {
+            e[j] = 1.0;
+            fapply(sym, v.g, v.C.data(), bct, e.data(), col.data());
+            for (int i = 0; i < nb; i++) LU[(size_t)i * nb + j] = col[i];
+            e[j] = 0.0;
+        }
+        double dmax = 0.0;
+        for (int i = 0; i < nb; i++) dmax = std::max(dmax, std::fabs(v.diag[i]));
+        piv.resize(nb);
+        for (int k = 0; k < nb; k++) {
+            int p = k;
+            for (int i = k + 1; i < nb; i++)
+                if (std::fabs(LU[(size_t)i * nb + k]) > std::fabs(LU[(size_t)p * nb + k])) p = i;
+            piv[k] = p;
+            if (!(std::fabs(LU[(size_t)p * nb + k]) > 1e-12 * dmax)) { LU.clear(); return; }
+            if (p != k)
+                for (int c = 0; c < nb; c++) std::swap(LU[(size_t)k * nb + c], LU[(size_t)p * nb + c]);
+            for (int i = k + 1; i < nb; i++) {
+                const double f = LU[(size_t)i * nb + k] / LU[(size_t)k * nb + k];
+                LU[(size_t)i * nb + k] = f;
+                for (int c = k + 1; c < nb; c++) LU[(size_t)i * nb + c] -= f * LU[(size_t)k * nb + c];
+            }
+        }
+        dense_ok = true;
+    }
+
+    void dense_solve(double* x, const double* b) {
+        const int nb = (int)piv.size();
+        std::vector<double> y(b, b + nb);
+        for (int k = 0; k < nb; k++) std::swap(y[k], y[piv[k]]);
+        for (int i = 0; i < nb; i++)
+            for (int c = 0; c < i; c++) y[i] -= LU[(size_t)i * nb + c] * y[c];
+        for (int i = nb - 1; i >= 0; i--) {
+            for (int c = i + 1; c < nb; c++) y[i] -= LU[(size_t)i * nb + c] * y[c];
+            y[i] /= LU[(size_t)i * nb + i];
+        }
+        for (int i = 0; i < nb; i++) x[i] = y[i];
+    }
+
     void bottom() {
         const int l = (int)L.size() - 1;
         Level& v = L[l];
+        if (o.bottom_solver == 1) {
+            if (!dense_tried) build_dense();
+            if (dense_ok) { dense_solve(v.cor.data(), v.res.data()); return; }
+        }
         std::fill(v.cor.begin(), v.cor.end(), 0.0);
+        if (o.bottom_solver == 2) {
+            smooth(l, o.final_smooth);
+            return;
+        }
         const int ret = bicgstab(l, v.cor.data(), v.res.data());
         if (ret != 0) {
             std::fill(v.cor.begin(), v.cor.end(), 0.0);
@@ -888,6 +958,7 @@ void orc_default_opts(orc_opts* o) {
     o->max_coarsening_level = -1;
     o->fixed_iter = -1;
     o->verbose = 0;
+    o->bottom_solver = 0;
 }
 
 // number of multigrid levels for a node grid (coarsen by 2 while every
@@ -906,6 +977,41 @@ int orc_num_levels(int nx, int ny, int nz, int max_coarsening_level) {
         lev++;
     }
     return lev;
+}
+
+// One V-cycle on A cor = res from cor = 0 on the fine level (for parity of
+// the multigrid cycle itself).
+void orc_vcycle(int sym, int nx, int ny, int nz, const double* dx, const double* C, const int* bc_type,
+                const orc_opts* opts, const double* res, double* cor) {
+    Hier H;
+    H.sym = sym;
+    H.bct = bc_type;
+    H.o = *opts;
+    const int nlev = orc_num_levels(nx, ny, nz, opts->max_coarsening_level);
+    const int nc = nc_of(sym);
+    H.L.resize(nlev);
+    for (int l = 0; l < nlev; l++) {
+        Level& v = H.L[l];
+        if (l == 0) v.g = mkgrid(nx, ny, nz, dx);
+        else {
+            const Grid& f = H.L[l - 1].g;
+            const double cdx[3] = {2 * f.dx[0], 2 * f.dx[1], 2 * f.dx[2]};
+            v.g = mkgrid((f.n[0] - 1) / 2 + 1, (f.n[1] - 1) / 2 + 1, (f.n[2] - 1) / 2 + 1, cdx);
+        }
+        const int64_t N = v.g.N();
+        v.C.resize(N * nc);
+        if (l == 0) std::memcpy(v.C.data(), C, sizeof(double) * N * nc);
+        else restrict_generic(H.L[l - 1].g, v.g, H.L[l - 1].C.data(), v.C.data(), nc, 1, nc, 1, nc);
+        v.diag.resize(3 * N);
+        diagonal(sym, v.g, v.C.data(), bc_type, v.diag.data());
+        v.res.assign(3 * N, 0.0);
+        v.cor.assign(3 * N, 0.0);
+        v.rescor.assign(3 * N, 0.0);
+    }
+    const int64_t n3 = 3 * H.L[0].g.N();
+    std::memcpy(H.L[0].res.data(), res, sizeof(double) * n3);
+    H.vcycle();
+    std::memcpy(cor, H.L[0].cor.data(), sizeof(double) * n3);
 }
 
 // Solve A sol = rhs (sol holds the initial guess on entry).  res_hist (may be

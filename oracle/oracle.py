@@ -36,6 +36,7 @@ class Opts(ctypes.Structure):
         ("max_coarsening_level", ctypes.c_int),
         ("fixed_iter", ctypes.c_int),
         ("verbose", ctypes.c_int),
+        ("bottom_solver", ctypes.c_int),
     ]
 
 
@@ -256,3 +257,20 @@ def derivative(which, f, dx):
     lib().orc_derivative.restype = None
     lib().orc_derivative(int(which), nx, ny, nz, _p(d), _p(np.ascontiguousarray(f)), _p(out))
     return out
+
+
+def vcycle(C, bc_type, res, dx, opts=None, **kw):
+    """One V-cycle on A cor = res from cor = 0."""
+    nx, ny, nz = _dims(C, vector=False)
+    o = opts if opts is not None else default_opts(**kw)
+    cor = np.empty_like(res)
+    d, bt = _dx(dx), _bct(bc_type)
+    lib().orc_vcycle.restype = None
+    lib().orc_vcycle(sym_of(C), nx, ny, nz, _p(d), _p(C), _p(bt), ctypes.byref(o), _p(res), _p(cor))
+    return cor
+
+
+def set_uniform(uniform):
+    """Operator::Elastic::SetUniform: True drops the grad-C term."""
+    lib().orc_set_uniform.restype = None
+    lib().orc_set_uniform(int(bool(uniform)))

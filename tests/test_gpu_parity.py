@@ -158,30 +158,103 @@ def test_vcycle_iterates_match(agb, oracle, case):
 
 @pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
 def test_solve_parity(agb, oracle, case):
+    """Config 1 runs V(2,2) cycles to 1e-10: same cycle count, same solution."""
     C, F0, bc, dx = CASES[case]()
     u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
-    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-12)
+    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10)
     assert rep_o.status == 0
     with make_op(agb, C, bc, dx) as op:
         u = u0.copy()
-        rep = agb.Newton(op).solve(u, b, F0, tol_rel=1e-12, tol_abs=0.0)
+        rep = agb.Newton(op).solve(u, b, F0, tol_rel=1e-10, tol_abs=0.0)
     assert rep["status"] == 0 and abs(rep["iters"] - rep_o.iters) <= 1
-    assert rep["final_resnorm"] <= 1e-12 * rep["rhsnorm0"]
+    assert rep["final_resnorm"] <= 1e-10 * rep["rhsnorm0"]
     assert rel(u, xo) <= 1e-8
+
+
+@pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm", "mm-randbc"])
+@pytest.mark.parametrize("bottom", ["bicgstab", "direct", "smoother"])
+def test_vcycle_parity(agb, oracle, case, bottom):
+    """One multigrid cycle (MLMG::mgVcycle) against the oracle's, with each
+    bottom solver and a 5^3-node bottom level; the FP32 cycle against the
+    FP64 one."""
+    C, F0, bc, dx = CASES[case]()
+    n = C.shape[0]
+    bt, _ = bc.tables()
+    r = P.random_field((3, n, n, n), 77)
+    mcl = oracle.num_levels(n, n, n) - 2
+    bs = {"bicgstab": 0, "direct": 1, "smoother": 2}[bottom]
+    with make_op(agb, C, bc, dx, max_coarsening_level=mcl, bottom_solver=bs) as op:
+        c64 = op.vcycle(r, precision="fp64")
+        c32 = op.vcycle(r, precision="mixed")
+    co = oracle.vcycle(C, bt, r, dx, max_coarsening_level=mcl, bottom_solver=bs)
+    # BiCGStab's relative stopping test makes its iteration count, and so the
+    # cycle's output, change at the 1e-6 level under 1e-15 perturbations of
+    # the input (the oracle shows the same); the other bottoms are exact.
+    assert rel(c64, co) <= (1e-4 if bottom == "bicgstab" else 1e-10)
+    assert rel(c32, c64) <= 1e-4
 
 
 @pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
 def test_mixed_precision_solve(agb, oracle, case):
+    """FP32 cycles inside FP64 refinement.  The stationary FP32 V-cycle
+    iteration is used on the polycrystal; on config 1 the reference's V-cycle
+    iteration has a growing mode (see test_reference_vcycle_instability), which
+    FP32 rounding excites, so config 1 runs the FGMRES(V-cycle) form."""
     C, F0, bc, dx = CASES[case]()
     u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
-    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-12)
-    with make_op(agb, C, bc, dx, precision=1) as op:
+    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10)
+    solver = 1 if case == "c1-iso" else 0
+    with make_op(agb, C, bc, dx, precision=1, solver=solver) as op:
         u = u0.copy()
         rep = agb.Newton(op).solve(u, b, F0, tol_rel=1e-10, tol_abs=0.0)
     assert rep["status"] == 0
     # the FP64 outer residual is what the tolerance is checked on
     assert rep["final_resnorm"] <= 1e-10 * rep["rhsnorm0"]
     assert rel(u, xo) <= 1e-7
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
+def test_fgmres_solve(agb, oracle, case, prec):
+    """FGMRES preconditioned by one V-cycle (FP64, or FP32 inside FP64
+    refinement) reaches the same solution as the oracle's V-cycle solve."""
+    C, F0, bc, dx = CASES[case]()
+    u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
+    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10)
+    with make_op(agb, C, bc, dx, solver=1, precision=prec, bottom_solver=1,
+                 max_coarsening_level=oracle.num_levels(*C.shape[:3]) - 2) as op:
+        u = u0.copy()
+        rep = agb.Newton(op).solve(u, b, F0, tol_rel=1e-10, tol_abs=0.0)
+    assert rep["status"] == 0 and rep["final_resnorm"] <= 1e-10 * rep["rhsnorm0"]
+    assert rep["iters"] < rep_o.iters
+    assert rel(u, xo) <= 1e-7
+
+
+def test_fgmres_where_vcycle_diverges(agb, oracle):
+    """Twelve stiff spheres (contrast 10) on a 9^3 grid: the operator has
+    eigenvalues with negative real part, the reference's stationary V-cycle
+    iteration diverges, FGMRES(V-cycle) converges to the dense solution of the
+    oracle's operator, in FP64 and in mixed precision."""
+    from alamo_gb300 import synth, bc as B
+    n = 9
+    C, F0, dx, _ = synth.spheres_iso(n, 12, seed=2, rmin=0.08, rmax=0.15)
+    bc = B.Constant()
+    u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
+    N3 = 3 * n ** 3
+    M = np.empty((N3, N3))
+    for q in range(N3):
+        e = np.zeros(N3)
+        e[q] = 1.0
+        M[:, q] = oracle.fapply(C, bt, e.reshape(3, n, n, n), dx).ravel()
+    xd = np.linalg.solve(M, rhs.ravel()).reshape(rhs.shape)
+    _, rep_v, hist = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_iter=60)
+    assert rep_v.status != 0 and hist[-1] > hist[0]  # the V-cycle iteration diverges here
+    for prec in (0, 1):
+        with make_op(agb, C, bc, dx, solver=1, precision=prec) as op:
+            u = u0.copy()
+            rep = agb.Newton(op).solve(u, b, F0, tol_rel=1e-10, tol_abs=0.0)
+        assert rep["status"] == 0
+        assert rel(u, xd) <= 1e-7
 
 
 def test_uniaxial_known_answer_gpu(agb):

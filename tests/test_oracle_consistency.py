@@ -61,3 +61,44 @@ def test_vcycle_converges_config1(oracle):
     x, rep, hist = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10)
     assert rep.status == 0 and rep.iters < 60
     assert hist[-1] <= 1e-10 * max(hist[0], np.abs(rhs).max())
+
+
+def test_reference_vcycle_instability(oracle):
+    """The reference's V-cycle iteration (damped Jacobi, rediscretised coarse
+    operators) on config 1 reaches ~4e-11 and then diverges: the
+    product-rule discretisation at the contrast-10 interface gives D^-1 A
+    eigenvalues with negative real part, which the smoother amplifies.  The
+    solver's FGMRES form exists for this; the plain V-cycle keeps the
+    reference's behaviour."""
+    C, F0, bc, dx = P.c1(33)
+    n = 33
+    bt, bv = bc.tables()
+    x = np.zeros((3, n, n, n))
+    rhs = oracle.build_rhs(C, F0, bt, x, oracle.bc_init(x, bt, bv), dx)
+    _, rep, hist = oracle.solve(C, bt, rhs, dx, fixed_iter=90)
+    h = hist / hist[0]
+    k = int(np.argmin(h))
+    assert h[k] < 1e-10 and 20 < k < 60
+    assert h[-1] > 1e3 * h[k]
+
+
+def test_negative_real_eigenvalues_small_inclusion(oracle):
+    """A 1.6-cell inclusion of contrast 10: D^-1 A has eigenvalues with
+    negative real part (no damped-Jacobi iteration can converge on them),
+    while contrast 3 keeps them all in the right half plane."""
+    from alamo_gb300 import synth
+    n = 9
+    dx = 1.0 / (n - 1)
+    out = {}
+    for con in (10.0, 3.0):
+        C, F0, _ = synth.inclusion_iso(n, radius=1.6 * dx, lam_in=con, mu_in=con)
+        bt, _ = __import__("alamo_gb300").bc.Constant().tables()
+        N3 = 3 * n ** 3
+        M = np.empty((N3, N3))
+        for q in range(N3):
+            e = np.zeros(N3)
+            e[q] = 1.0
+            M[:, q] = oracle.fapply(C, bt, e.reshape(3, n, n, n), dx).ravel()
+        d = oracle.diagonal(C, bt, dx).ravel()
+        out[con] = np.linalg.eigvals(M / d[:, None]).real.min()
+    assert out[10.0] < 0 < out[3.0]
