@@ -53,6 +53,8 @@ class SolverOpts(ctypes.Structure):
         ("krylov_dim", ctypes.c_int),
         ("inner_tol", ctypes.c_double),
         ("bottom_solver", ctypes.c_int),
+        ("fine_kernel", ctypes.c_int),
+        ("krylov_reorth", ctypes.c_int),
         ("reserved_opts", ctypes.c_int),
     ]
 

@@ -353,6 +353,13 @@ struct Fam<double> { enum { J = AGB_K_JACOBI_F64, R = AGB_K_RESIDUAL_F64 }; };
 template <>
 struct Fam<float> { enum { J = AGB_K_JACOBI_F32, R = AGB_K_RESIDUAL_F32 }; };
 
+// the z-marching kernels serve the FP32 fine level (FP64 stays on the
+// per-node kernels: it is FP64-pipe bound and the z-march form spills)
+template <typename T>
+bool use_zm(const agb_elastic*, int) { return false; }
+template <>
+bool use_zm<float>(const agb_elastic* h, int l) { return l == 0 && h->opts.fine_kernel == 0; }
+
 // ncalls Fsmooth calls (2 sweeps each) on level l; cor_zero: cor is known 0
 template <typename T>
 agb_status smooth(agb_elastic* h, std::vector<Lev<T>>& L, int l, int ncalls, bool cor_zero) {
@@ -366,8 +373,11 @@ agb_status smooth(agb_elastic* h, std::vector<Lev<T>>& L, int l, int ncalls, boo
     for (int s = 0; s < sweeps; s++) {
         {
             ProfScope ps(h, Fam<T>::J, l == 0 && !(cor_zero && s == 0));
-            CK(launch_jacobi<T>(h->sym, (cor_zero && s == 0) ? nullptr : v.cor, v.res, v.diag, v.C, v.G, h->bc, w,
-                                v.tmp, h->stream));
+            if (use_zm<T>(h, l) && !(cor_zero && s == 0))
+                CK(launch_zmarch<T>(1, h->sym, v.cor, v.C, v.G, h->bc, v.res, v.diag, w, v.tmp, h->stream));
+            else
+                CK(launch_jacobi<T>(h->sym, (cor_zero && s == 0) ? nullptr : v.cor, v.res, v.diag, v.C, v.G, h->bc,
+                                    w, v.tmp, h->stream));
         }
         h->launches++;
         std::swap(v.cor, v.tmp);
@@ -424,7 +434,10 @@ agb_status vcycle(agb_elastic* h, std::vector<Lev<T>>& L) {
         TRY(smooth<T>(h, L, l, h->opts.pre_smooth, true));
         {
             ProfScope ps(h, Fam<T>::R, l == 0);
-            CK(launch_residual<T>(h->sym, v.cor, v.res, v.C, v.G, h->bc, v.rescor, nullptr, nullptr, h->stream));
+            if (use_zm<T>(h, l))
+                CK(launch_zmarch<T>(2, h->sym, v.cor, v.C, v.G, h->bc, v.res, nullptr, T(0), v.rescor, h->stream));
+            else
+                CK(launch_residual<T>(h->sym, v.cor, v.res, v.C, v.G, h->bc, v.rescor, nullptr, nullptr, h->stream));
         }
         {
             ProfScope ps(h, AGB_K_RESTRICT, l == 0);
@@ -543,17 +556,23 @@ agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, doub
         TRY(vcycle<T>(h, L));
         CK(cudaMemcpyAsync(K.Z[j], top.cor, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
         // w = A Z_j
-        CK(launch_fapply<T>(h->sym, K.Z[j], top.C, top.G, h->bc, K.w, st));
-        // CGS2
+        if (use_zm<T>(h, 0))
+            CK(launch_zmarch<T>(0, h->sym, K.Z[j], top.C, top.G, h->bc, nullptr, nullptr, T(0), K.w, st));
+        else
+            CK(launch_fapply<T>(h->sym, K.Z[j], top.C, top.G, h->bc, K.w, st));
+        // classical Gram-Schmidt, re-orthogonalised once unless krylov_reorth = 0
         CK(launch_multidot<T>(K.Vdev, j + 1, K.w, n, K.part, K.dots, st));
         CK(launch_multiaxpy<T>(K.w, 1.0, K.Vdev, K.dots, -1.0, j + 1, n, st));
-        CK(launch_multidot<T>(K.Vdev, j + 1, K.w, n, K.part, K.dots + 40, st));
-        CK(launch_multiaxpy<T>(K.w, 1.0, K.Vdev, K.dots + 40, -1.0, j + 1, n, st));
+        const bool reorth = h->opts.krylov_reorth != 0;
+        if (reorth) {
+            CK(launch_multidot<T>(K.Vdev, j + 1, K.w, n, K.part, K.dots + 40, st));
+            CK(launch_multiaxpy<T>(K.w, 1.0, K.Vdev, K.dots + 40, -1.0, j + 1, n, st));
+        }
         CK(launch_multidot<T>(K.Wdev, 1, K.w, n, K.part, K.dots + 80, st));
         CK(cudaMemcpyAsync(K.hdots, K.dots, sizeof(double) * 120, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        h->launches += 12;
-        for (int i = 0; i <= j; i++) H[(size_t)i * m + j] = K.hdots[i] + K.hdots[40 + i];
+        h->launches += reorth ? 12 : 8;
+        for (int i = 0; i <= j; i++) H[(size_t)i * m + j] = K.hdots[i] + (reorth ? K.hdots[40 + i] : 0.0);
         const double hn = std::sqrt(std::max(K.hdots[80], 0.0));
         H[(size_t)(j + 1) * m + j] = hn;
         if (hn > 0.0) {
@@ -749,6 +768,8 @@ agb_status agb_default_opts(agb_solver_opts* o) {
     o->krylov_dim = 20;
     o->inner_tol = 1e-4;
     o->bottom_solver = AGB_BOTTOM_BICGSTAB;
+    o->fine_kernel = 0;
+    o->krylov_reorth = 1;
     o->reserved_opts = 0;
     return AGB_OK;
 }
@@ -965,7 +986,11 @@ agb_status agb_elastic_fapply_f32(agb_elastic* h, int level, const float* u, flo
     TRY(dev_out(h, 1, f, bytes, where, &df));
     {
         ProfScope ps(h, AGB_K_FAPPLY_F32, level == 0);
-        CK(launch_fapply<float>(h->sym, (const float*)du, v.C, v.G, h->bc, (float*)df, h->stream));
+        if (use_zm<float>(h, level))
+            CK(launch_zmarch<float>(0, h->sym, (const float*)du, v.C, v.G, h->bc, nullptr, nullptr, 0.f, (float*)df,
+                                    h->stream));
+        else
+            CK(launch_fapply<float>(h->sym, (const float*)du, v.C, v.G, h->bc, (float*)df, h->stream));
     }
     h->launches++;
     TRY(finish_out(h, f, df, bytes, where));

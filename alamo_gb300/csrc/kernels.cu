@@ -569,33 +569,43 @@ namespace agb {
 
 // ---------------------------------------------------------------- Krylov
 // out[i] = sum_q V_i[q] * w[q] for i < k (FP64 accumulation), two passes:
-// per-block partial sums, then one block per i over the partials.
+// per-block partial sums, then one block per i over the partials.  Blocks
+// are organised as (element range) x (chunk of 8 vectors) so the 8
+// accumulators of a thread stay in registers.
 static constexpr int KMAX = 40;
+static constexpr int KCH = 8;
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_multidot_partial(const T* const* __restrict__ V, int k, const T* __restrict__ w,
                                                           int64_t n, double* __restrict__ part) {
-    double acc[KMAX];
+    const int c0 = blockIdx.y * KCH;
+    __shared__ const T* vp[KCH];
+    if (threadIdx.x < KCH) vp[threadIdx.x] = (c0 + (int)threadIdx.x < k) ? V[c0 + threadIdx.x] : nullptr;
+    __syncthreads();
+    const int kk = min(KCH, k - c0);
+    double acc[KCH];
 #pragma unroll
-    for (int i = 0; i < KMAX; i++) acc[i] = 0.0;
+    for (int i = 0; i < KCH; i++) acc[i] = 0.0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
         const double wq = (double)w[q];
-#pragma unroll 4
-        for (int i = 0; i < k; i++) acc[i] += (double)V[i][q] * wq;
+#pragma unroll
+        for (int i = 0; i < KCH; i++)
+            if (i < kk) acc[i] += (double)vp[i][q] * wq;
     }
-    __shared__ double sh[8][KMAX];
+    __shared__ double sh[8][KCH];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int i = 0; i < k; i++) {
+#pragma unroll
+    for (int i = 0; i < KCH; i++) {
         double v = acc[i];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) sh[wid][i] = v;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < k; i += blockDim.x) {
-        double s = 0.0;
-        for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += sh[q][i];
-        part[(int64_t)blockIdx.x * KMAX + i] = s;
+    if (threadIdx.x < kk) {
+        double t = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[q][threadIdx.x];
+        part[(int64_t)blockIdx.x * KMAX + c0 + threadIdx.x] = t;
     }
 }
 
@@ -622,7 +632,8 @@ cudaError_t launch_multidot(const T* const* V, int k, const T* w, int64_t n, dou
                             cudaStream_t s) {
     if (k < 1 || k > KMAX) return cudaErrorInvalidValue;
     const int nb = multidot_blocks();
-    k_multidot_partial<T><<<nb, 256, 0, s>>>(V, k, w, n, part);
+    dim3 grd(nb, (k + KCH - 1) / KCH);
+    k_multidot_partial<T><<<grd, 256, 0, s>>>(V, k, w, n, part);
     k_multidot_final<<<k, 256, 0, s>>>(part, nb, k, out);
     return cudaGetLastError();
 }
@@ -631,17 +642,29 @@ template cudaError_t launch_multidot<double>(const double* const*, int, const do
 template cudaError_t launch_multidot<float>(const float* const*, int, const float*, int64_t, double*, double*,
                                             cudaStream_t);
 
-// w = beta * w + sum_i coef[i] * scale * V_i  (coef in device memory)
+// w = beta * w + sum_i coef[i] * scale * V_i  (coef in device memory); two
+// elements per thread, pointer table and coefficients in shared memory
 template <typename T>
 __global__ void __launch_bounds__(256) k_multiaxpy(T* __restrict__ w, double beta, const T* const* __restrict__ V,
                                                    const double* __restrict__ coef, double scale, int k, int64_t n) {
     __shared__ double c[KMAX];
-    for (int i = threadIdx.x; i < k; i += blockDim.x) c[i] = coef[i] * scale;
+    __shared__ const T* vp[KMAX];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) { c[i] = coef[i] * scale; vp[i] = V[i]; }
     __syncthreads();
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        double acc = (beta == 0.0) ? 0.0 : beta * (double)w[q];
-        for (int i = 0; i < k; i++) acc += c[i] * (double)V[i][q];
-        w[q] = (T)acc;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += 2 * stride) {
+        const int64_t q2 = q + stride;
+        const bool two = q2 < n;
+        double a0 = (beta == 0.0) ? 0.0 : beta * (double)w[q];
+        double a1 = (two && beta != 0.0) ? beta * (double)w[q2] : 0.0;
+        for (int i = 0; i < k; i++) {
+            const T* v = vp[i];
+            const double ci = c[i];
+            a0 += ci * (double)v[q];
+            if (two) a1 += ci * (double)v[q2];
+        }
+        w[q] = (T)a0;
+        if (two) w[q2] = (T)a1;
     }
 }
 

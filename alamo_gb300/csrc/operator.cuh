@@ -127,19 +127,22 @@ __device__ __forceinline__ void apply_boundary(const T* __restrict__ u, const Le
     for (int r = 0; r < 3; r++) f[r] = bc_component<T>(bc, reg, r, u[r * G.N + id], g, s, n);
 }
 
-// Apply the operator at an interior node.  C is SoA: C[k * N + node].
-template <typename T, int SYM>
-__device__ __forceinline__ void apply_interior(const T* __restrict__ u, const T* __restrict__ C, const LevelGeom<T>& G,
-                                               int64_t id, T f[3]) {
-    const int64_t sx = 1, sy = G.sy, sz = G.sz, N = G.N;
+// Interior-node arithmetic with the displacement and the stiffness read
+// through accessors: U(p, a, b, c) is component p of u at node offset
+// (a, b, c) in {-1, 0, 1}^3 and Cf(e, a, b, c) is stiffness entry e at an
+// offset with at most one non-zero axis.  Offsets and entries are
+// compile-time constants once the loops unroll, so the accessors cost nothing
+// beyond their loads.
+template <typename T, int SYM, typename UA, typename CA>
+__device__ __forceinline__ void interior_rows(UA U, CA Cf, const LevelGeom<T>& G, T f[3]) {
     T g[3][3];
     // Hessian of each component: xx, yy, zz, xy, xz, yz
     T H[3][6];
 #pragma unroll
     for (int p = 0; p < 3; p++) {
-        const T* up = u + p * N + id;
-        const T c0 = up[0];
-        const T xp = up[sx], xm = up[-sx], yp = up[sy], ym = up[-sy], zp = up[sz], zm = up[-sz];
+        const T c0 = U(p, 0, 0, 0);
+        const T xp = U(p, 1, 0, 0), xm = U(p, -1, 0, 0), yp = U(p, 0, 1, 0), ym = U(p, 0, -1, 0);
+        const T zp = U(p, 0, 0, 1), zm = U(p, 0, 0, -1);
         g[p][0] = (xp - xm) * G.h[0];
         g[p][1] = (yp - ym) * G.h[1];
         g[p][2] = (zp - zm) * G.h[2];
@@ -147,26 +150,23 @@ __device__ __forceinline__ void apply_interior(const T* __restrict__ u, const T*
         H[p][0] = ((xp + xm) - c2) * G.i2[0];
         H[p][1] = ((yp + ym) - c2) * G.i2[1];
         H[p][2] = ((zp + zm) - c2) * G.i2[2];
-        H[p][3] = ((up[sx + sy] + up[-sx - sy]) - (up[sx - sy] + up[-sx + sy])) * G.q[0];
-        H[p][4] = ((up[sx + sz] + up[-sx - sz]) - (up[sx - sz] + up[-sx + sz])) * G.q[1];
-        H[p][5] = ((up[sy + sz] + up[-sy - sz]) - (up[sy - sz] + up[-sy + sz])) * G.q[2];
+        H[p][3] = ((U(p, 1, 1, 0) + U(p, -1, -1, 0)) - (U(p, 1, -1, 0) + U(p, -1, 1, 0))) * G.q[0];
+        H[p][4] = ((U(p, 1, 0, 1) + U(p, -1, 0, -1)) - (U(p, 1, 0, -1) + U(p, -1, 0, 1))) * G.q[1];
+        H[p][5] = ((U(p, 0, 1, 1) + U(p, 0, -1, -1)) - (U(p, 0, 1, -1) + U(p, 0, -1, 1))) * G.q[2];
     }
     enum { XX = 0, YY = 1, ZZ = 2, XY = 3, XZ = 4, YZ = 5 };
-    const int64_t off[3] = {sx, sy, sz};
     if (SYM == SYM_ISO) {
-        const T l = C[id], m = C[N + id];
+        const T l = Cf(0, 0, 0, 0), m = Cf(1, 0, 0, 0);
         const T lm = l + m;
         f[0] = m * (H[0][XX] + H[0][YY] + H[0][ZZ]) + lm * (H[0][XX] + H[1][XY] + H[2][XZ]);
         f[1] = m * (H[1][XX] + H[1][YY] + H[1][ZZ]) + lm * (H[0][XY] + H[1][YY] + H[2][YZ]);
         f[2] = m * (H[2][XX] + H[2][YY] + H[2][ZZ]) + lm * (H[0][XZ] + H[1][YZ] + H[2][ZZ]);
         // grad C term: f_i += dl_i tr(g) + sum_q dm_q (g_iq + g_qi)
         const T tr = g[0][0] + g[1][1] + g[2][2];
-        T dl[3], dm[3];
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-            dl[q] = (C[id + off[q]] - C[id - off[q]]) * G.h[q];
-            dm[q] = (C[N + id + off[q]] - C[N + id - off[q]]) * G.h[q];
-        }
+        const T dl[3] = {(Cf(0, 1, 0, 0) - Cf(0, -1, 0, 0)) * G.h[0], (Cf(0, 0, 1, 0) - Cf(0, 0, -1, 0)) * G.h[1],
+                         (Cf(0, 0, 0, 1) - Cf(0, 0, 0, -1)) * G.h[2]};
+        const T dm[3] = {(Cf(1, 1, 0, 0) - Cf(1, -1, 0, 0)) * G.h[0], (Cf(1, 0, 1, 0) - Cf(1, 0, -1, 0)) * G.h[1],
+                         (Cf(1, 0, 0, 1) - Cf(1, 0, 0, -1)) * G.h[2]};
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             T t = dl[i] * tr;
@@ -177,7 +177,7 @@ __device__ __forceinline__ void apply_interior(const T* __restrict__ u, const T*
     } else {
         T d[21];
 #pragma unroll
-        for (int a = 0; a < 21; a++) d[a] = C[a * N + id];
+        for (int a = 0; a < 21; a++) d[a] = Cf(a, 0, 0, 0);
         // C : grad grad u (the grouping of src/Set/Matrix4_MajorMinor.H:709-767)
         f[0] = d[0] * H[0][XX] + d[1] * (H[0][XY] + H[0][XY] + H[1][XX]) + d[2] * (H[0][XZ] + H[0][XZ] + H[2][XX]) +
                d[3] * H[1][XY] + d[4] * (H[1][XZ] + H[2][XY]) + d[5] * H[2][XZ] + d[6] * (H[0][YY] + H[1][XY]) +
@@ -199,14 +199,15 @@ __device__ __forceinline__ void apply_interior(const T* __restrict__ u, const T*
         T col[3][3];
 #pragma unroll
         for (int q = 0; q < 3; q++) {
+            const int ox = q == 0, oy = q == 1, oz = q == 2;
 #pragma unroll
             for (int i = 0; i < 3; i++) {
                 const int a = pair_of(i, q);
                 T acc = T(0);
 #pragma unroll
-                for (int b = 0; b < 6; b++) {
-                    const int e = mm_ut(a, b);
-                    acc += (C[e * N + id + off[q]] - C[e * N + id - off[q]]) * v[b];
+                for (int bb = 0; bb < 6; bb++) {
+                    const int e = mm_ut(a, bb);
+                    acc += (Cf(e, ox, oy, oz) - Cf(e, -ox, -oy, -oz)) * v[bb];
                 }
                 col[q][i] = acc * G.h[q];
             }
@@ -214,6 +215,17 @@ __device__ __forceinline__ void apply_interior(const T* __restrict__ u, const T*
 #pragma unroll
         for (int i = 0; i < 3; i++) f[i] += (col[0][i] + col[1][i]) + col[2][i];
     }
+}
+
+// Apply the operator at an interior node, everything read from global
+// memory.  C is SoA: C[k * N + node].
+template <typename T, int SYM>
+__device__ __forceinline__ void apply_interior(const T* __restrict__ u, const T* __restrict__ C, const LevelGeom<T>& G,
+                                               int64_t id, T f[3]) {
+    const int64_t N = G.N, sy = G.sy, sz = G.sz;
+    auto U = [&](int p, int a, int b, int c) { return u[p * N + id + a + sy * b + sz * c]; };
+    auto Cf = [&](int e, int a, int b, int c) { return C[e * N + id + a + sy * b + sz * c]; };
+    interior_rows<T, SYM>(U, Cf, G, f);
 }
 
 // Apply the operator at any node.

@@ -6,10 +6,13 @@ rotations), uniaxial_stress_clamp loading u_x = 0.01 on the x+ face; stiffness
 is major-minor (21 values per node).  Synthetic inputs, seeded.
 
 One step = one complete solve from the inputs resident in HBM: SetModel
-(stiffness layout change), prepareForSolve (stiffness coarsening, diagonals),
-the Newton right-hand side and the multigrid solve to 1e-8 relative residual
-(inf-norm, tol_abs = 0), fast path = FP32 V-cycles inside FP64 iterative
-refinement.  `value` is seconds per solve (lower is better); `e2e` is the same
+(stiffness layout change), prepareForSolve (stiffness coarsening, diagonals,
+bottom-level inverse), the Newton right-hand side and the solve to 1e-8
+relative residual (inf-norm of the FP64 residual, tol_abs = 0).  Fast path:
+FGMRES preconditioned by one V-cycle, both in FP32, inside FP64 iterative
+refinement, with a direct solve on a 5^3-node bottom level.  The plain FP64
+comparison is the reference's algorithm on the GPU: V(2,2) cycles with
+damped Jacobi and the BiCGStab bottom, everything FP64.  `value` is seconds per solve (lower is better); `e2e` is the same
 solve through the C ABI with host buffers (stiffness and right-hand side
 copied in, displacement copied out, inside the timed region).  The plain FP64
 V-cycle solve of the same input is timed beside it (`plain_fp64_s`).
@@ -33,7 +36,7 @@ sys.path.insert(0, ROOT)
 # FP64 V-cycles the reference algorithm needs to reach 1e-8 on each workload
 # (the oracle and the GPU FP64 path iterate identically); used to scale the
 # CPU sample to a whole solve.
-FP64_CYCLES = {"c1": 17, "c2": 31, "c3": 20}
+FP64_CYCLES = {"c1": 25, "c2": 87, "c3": None}
 
 # bytes each kernel family must move per fine-level node (each array once)
 BYTES_PER_NODE = {
@@ -59,7 +62,10 @@ def parse():
     p.add_argument("--impl", default="agb", choices=["agb", "reference"])
     p.add_argument("--config", default="c2", choices=["c1", "c2", "c3"])
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    p.add_argument("--inner", type=int, default=2, help="FP32 V-cycles per FP64 residual")
+    p.add_argument("--solver", default="fgmres", choices=["fgmres", "vcycle"])
+    p.add_argument("--inner", type=int, default=2, help="FP32 V-cycles per FP64 residual (vcycle solver)")
+    p.add_argument("--inner-tol", type=float, default=1e-4, help="FP32 FGMRES reduction per FP64 residual")
+    p.add_argument("--krylov", type=int, default=20)
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison solve")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-e2e", action="store_true")
@@ -235,7 +241,13 @@ def main():
     nc = C.shape[-1]
     sym = "isotropic" if nc == 2 else "majorminor"
     prec = 1 if args.precision == "mixed" else 0
-    opts = A.default_opts(precision=prec, inner_cycles=args.inner)
+    nlev = 1
+    m = n
+    while (m - 1) % 2 == 0 and (m - 1) // 2 >= 2:
+        m = (m - 1) // 2 + 1
+        nlev += 1
+    opts = A.default_opts(precision=prec, inner_cycles=args.inner, solver=args.solver, inner_tol=args.inner_tol,
+                          krylov_dim=args.krylov, bottom_solver="direct", max_coarsening_level=max(nlev - 2, 0))
     op = A.Elastic(n, dx, sym, opts)
     stream = torch.cuda.Stream()
     _lib.check(_lib.lib().agb_elastic_set_stream(op.h, __import__("ctypes").c_void_p(stream.cuda_stream)))
@@ -382,11 +394,13 @@ def main():
         "value": sec, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-cycle/f64-refinement" if prec else "f64", "data": "synthetic",
-        "config": {"workload": name, "nodes": N, "precision": args.precision, "inner_cycles": args.inner,
+        "config": {"workload": name, "nodes": N, "precision": args.precision, "solver": args.solver,
+                   "inner_tol": args.inner_tol, "krylov_dim": args.krylov, "bottom": "direct 5^3",
                    "parallelism": "replicas" if world > 1 else "single-gpu",
                    "l2": "inputs larger than L2 (%.1f GB of stiffness)" % (C.nbytes / 1e9)},
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": ck,
         "solve": {"v_cycles": rep.get("iters"), "fp64_residuals": rep.get("fp64_residuals"),
+                  "final_rel_resnorm_l2": (rep.get("final_resnorm_l2", 0) / rep["rhsnorm_l2"]) if rep else None,
                   "final_rel_resnorm": (rep.get("final_resnorm", 0) / rep["rhsnorm0"]) if rep else None,
                   "levels": rep.get("nlevels")},
         "plain_fp64": plain, "speedup_vs_plain_fp64": (plain["seconds"] / sec) if plain else None,

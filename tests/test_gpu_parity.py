@@ -194,6 +194,22 @@ def test_vcycle_parity(agb, oracle, case, bottom):
     assert rel(c32, c64) <= 1e-4
 
 
+@pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm", "iso-randbc", "mm-randbc"])
+def test_zmarch_matches_per_node_kernels(agb, oracle, case):
+    """The FP32 fine-level z-marching kernels (Fapply, Jacobi sweep,
+    residual) against the one-thread-per-node kernels: one FP32 V-cycle and
+    one FP32 Fapply give the same numbers to FP32 rounding."""
+    C, F0, bc, dx = CASES[case]()
+    n = C.shape[0]
+    r = P.random_field((3, n, n, n), 91)
+    outs = []
+    for fk in (0, 1):
+        with make_op(agb, C, bc, dx, fine_kernel=fk) as op:
+            outs.append((op.vcycle(r, precision="mixed"), op.Fapply_f32(r.astype(np.float32))))
+    assert rel(outs[0][1], outs[1][1]) <= 1e-6
+    assert rel(outs[0][0], outs[1][0]) <= 1e-5
+
+
 @pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
 def test_mixed_precision_solve(agb, oracle, case):
     """FP32 cycles inside FP64 refinement.  The stationary FP32 V-cycle
