@@ -769,7 +769,7 @@ agb_status agb_default_opts(agb_solver_opts* o) {
     o->inner_tol = 1e-4;
     o->bottom_solver = AGB_BOTTOM_BICGSTAB;
     o->fine_kernel = 0;
-    o->krylov_reorth = 1;
+    o->krylov_reorth = 0;
     o->reserved_opts = 0;
     return AGB_OK;
 }

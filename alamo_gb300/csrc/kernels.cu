@@ -575,6 +575,9 @@ namespace agb {
 static constexpr int KMAX = 40;
 static constexpr int KCH = 8;
 
+// Per-thread sums run in the vectors' own type (FP32 vectors: FP32 FMA, the
+// 1/64-rate FP64 pipe of GB300 would bound the kernel); the cross-thread
+// and cross-block reductions run in FP64.
 template <typename T>
 __global__ void __launch_bounds__(256) k_multidot_partial(const T* const* __restrict__ V, int k, const T* __restrict__ w,
                                                           int64_t n, double* __restrict__ part) {
@@ -583,20 +586,20 @@ __global__ void __launch_bounds__(256) k_multidot_partial(const T* const* __rest
     if (threadIdx.x < KCH) vp[threadIdx.x] = (c0 + (int)threadIdx.x < k) ? V[c0 + threadIdx.x] : nullptr;
     __syncthreads();
     const int kk = min(KCH, k - c0);
-    double acc[KCH];
+    T acc[KCH];
 #pragma unroll
-    for (int i = 0; i < KCH; i++) acc[i] = 0.0;
+    for (int i = 0; i < KCH; i++) acc[i] = T(0);
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const double wq = (double)w[q];
+        const T wq = w[q];
 #pragma unroll
         for (int i = 0; i < KCH; i++)
-            if (i < kk) acc[i] += (double)vp[i][q] * wq;
+            if (i < kk) acc[i] += vp[i][q] * wq;
     }
     __shared__ double sh[8][KCH];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < KCH; i++) {
-        double v = acc[i];
+        double v = (double)acc[i];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) sh[wid][i] = v;
@@ -643,28 +646,30 @@ template cudaError_t launch_multidot<float>(const float* const*, int, const floa
                                             cudaStream_t);
 
 // w = beta * w + sum_i coef[i] * scale * V_i  (coef in device memory); two
-// elements per thread, pointer table and coefficients in shared memory
+// elements per thread, pointer table and coefficients in shared memory,
+// arithmetic in the vectors' type
 template <typename T>
 __global__ void __launch_bounds__(256) k_multiaxpy(T* __restrict__ w, double beta, const T* const* __restrict__ V,
                                                    const double* __restrict__ coef, double scale, int k, int64_t n) {
-    __shared__ double c[KMAX];
+    __shared__ T c[KMAX];
     __shared__ const T* vp[KMAX];
-    for (int i = threadIdx.x; i < k; i += blockDim.x) { c[i] = coef[i] * scale; vp[i] = V[i]; }
+    for (int i = threadIdx.x; i < k; i += blockDim.x) { c[i] = (T)(coef[i] * scale); vp[i] = V[i]; }
     __syncthreads();
+    const T bt = (T)beta;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += 2 * stride) {
         const int64_t q2 = q + stride;
         const bool two = q2 < n;
-        double a0 = (beta == 0.0) ? 0.0 : beta * (double)w[q];
-        double a1 = (two && beta != 0.0) ? beta * (double)w[q2] : 0.0;
+        T a0 = (beta == 0.0) ? T(0) : bt * w[q];
+        T a1 = (two && beta != 0.0) ? bt * w[q2] : T(0);
         for (int i = 0; i < k; i++) {
             const T* v = vp[i];
-            const double ci = c[i];
-            a0 += ci * (double)v[q];
-            if (two) a1 += ci * (double)v[q2];
+            const T ci = c[i];
+            a0 += ci * v[q];
+            if (two) a1 += ci * v[q2];
         }
-        w[q] = (T)a0;
-        if (two) w[q2] = (T)a1;
+        w[q] = a0;
+        if (two) w[q2] = a1;
     }
 }
 

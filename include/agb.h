@@ -89,7 +89,7 @@ typedef struct agb_solver_opts {
     double inner_tol;         /* mixed FGMRES: residual reduction of one FP32 inner solve (1e-4) */
     int bottom_solver;        /* agb_bottom_solver (AGB_BOTTOM_BICGSTAB) */
     int fine_kernel;          /* FP32 fine-level stencil kernels: 0 z-marching (default), 1 one thread per node */
-    int krylov_reorth;        /* FGMRES Gram-Schmidt: 1 re-orthogonalise once (default), 0 single pass */
+    int krylov_reorth;        /* FGMRES Gram-Schmidt: 1 re-orthogonalise once, 0 single pass (default) */
     int reserved_opts;
 } agb_solver_opts;
 
