@@ -19,7 +19,7 @@ EXPORTS = [
     "agb_linear_solve", "agb_newton_solve", "agb_elastic_stress_strain", "agb_profile_enable",
     "agb_profile_reset", "agb_profile_get", "agb_launch_count", "agb_cubic_stiffness", "agb_synth_uniform",
     "agb_synth_inclusion_iso", "agb_synth_voronoi_cubic", "agb_synth_spheres_iso", "agb_status_string",
-    "agb_last_error", "agb_version",
+    "agb_last_error", "agb_version", "agb_residual_norms_noalloc",
 ]
 
 AGB_OK, AGB_NOT_CONVERGED, AGB_NAN, AGB_BAD_ARG, AGB_CUDA_ERROR, AGB_NOT_READY, AGB_OUT_OF_MEMORY, AGB_LIMIT = range(8)

@@ -123,3 +123,8 @@ template <typename T>
 cudaError_t launch_zmarch(int mode, int sym, const T* x, const T* C, const LevelGeom<T>& G, const BcTable& bc,
                           const T* b, const T* dg, T omega, T* out, cudaStream_t s);
 }  // namespace agb
+
+namespace agb {
+// message returned by agb_last_error() for the calling thread
+void set_last_error(const char* msg);
+}  // namespace agb

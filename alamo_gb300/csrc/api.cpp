@@ -745,6 +745,10 @@ agb_status check_level(agb_elastic* h, int level) {
 
 }  // namespace
 
+namespace agb {
+void set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+}  // namespace agb
+
 // ============================================================================
 extern "C" {
 

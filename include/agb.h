@@ -202,6 +202,27 @@ agb_status agb_newton_solve(agb_elastic* h, double* u, const double* b, const do
 agb_status agb_elastic_stress_strain(agb_elastic* h, const double* u, const double* F0, int f0_ncomp,
                                      double* stress, double* strain, double* energy, int where);
 
+/* ------------------------------------------------ allocation-free call */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (inside a CUDA graph capture, inside another library's memory pool, or in
+ * a host code that reserves the device up front): r = b - A x and its norms
+ * {||r||_inf, ||r||_2} with no allocation and no handle.  The caller passes
+ * device arrays only: C_soa is the per-node stiffness split per component
+ * (2 or 21 arrays of nx*ny*nz doubles one after another), bc_type the 26*3
+ * table of agb_elastic_set_bc, x, b, r vector fields (3*N doubles); norms is
+ * host memory.  The per-block partial norms live in a fixed 2 MiB device
+ * array inside the library (AGB_NOALLOC_MAX_BLOCKS pairs of doubles, one per
+ * 32x4x2-node block, held by every GPU that loads the library until exit), so
+ * grids of more than AGB_NOALLOC_MAX_BLOCKS blocks (about 33.5M nodes) return
+ * AGB_LIMIT.  The first call on a device looks the array's address up and
+ * must come before any stream capture on that device.  Calls share the
+ * array: calls that overlap on the GPU race and give wrong norms.  Runs on
+ * `stream` (NULL: the legacy default stream) and returns after it. */
+#define AGB_NOALLOC_MAX_BLOCKS 131072
+agb_status agb_residual_norms_noalloc(int nx, int ny, int nz, const double dx[3], int sym, const double* C_soa,
+                                      const int* bc_type, const double* x, const double* b, double* r,
+                                      double norms[2], void* stream);
+
 /* --------------------------------------------------------- profiling */
 /* Kernel families timed with CUDA events on the handle's stream when
  * profiling is on (fine level only). */
