@@ -85,7 +85,8 @@ cudaError_t launch_bottom_bicgstab(int sym, const double* C, const double* diag,
 }  // namespace agb
 
 namespace agb {
-// Krylov helpers (FP64 accumulation for every type)
+// Krylov helpers (FP64 block and grid reductions; FP32 vectors summed in
+// compensated FP32 within a thread)
 int multidot_blocks();
 // out[i] = <V_i, w>, i < k <= 40; part: multidot_blocks() * 40 doubles
 template <typename T>
@@ -95,6 +96,10 @@ cudaError_t launch_multidot(const T* const* V, int k, const T* w, int64_t n, dou
 template <typename T>
 cudaError_t launch_multiaxpy(T* w, double beta, const T* const* V, const double* coef, double scale, int k, int64_t n,
                              cudaStream_t s);
+// the same, also norm2[0] = ||w_new||_2^2 (part: multidot_blocks() * 40 doubles)
+template <typename T>
+cudaError_t launch_multiaxpy_norm(T* w, double beta, const T* const* V, const double* coef, double scale, int k,
+                                  int64_t n, double* part, double* norm2, cudaStream_t s);
 // every elementwise helper takes (inputs, outputs, n, scale)
 // dst = a * src
 template <typename T>

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "agb_launch.h"
+#include "zmarch_tma.h"
 
 using namespace agb;
 
@@ -119,6 +120,11 @@ struct agb_elastic {
     double* dw = nullptr;  // 9N scratch of the Newton RHS
     Krylov<double> K64;
     Krylov<float> K32;
+    // FP32 fine-level stiffness with a padded x pitch and its TMA map
+    // (interior stencil kernels of fine_kernel 0)
+    float* c32pad = nullptr;
+    CUtensorMap cmap{};
+    bool have_cmap = false;
     // dense direct bottom solve
     double* bot_inv = nullptr;
     int bot_nb = 0;
@@ -302,6 +308,46 @@ agb_status build_bottom_dense(agb_elastic* h) {
 }
 
 // ---------------------------------------------------------------- prepare
+void free_pad(agb_elastic* h) {
+    cudaFree(h->c32pad);
+    h->c32pad = nullptr;
+    h->have_cmap = false;
+}
+
+// FP32 copies of every level's stiffness and diagonal; for the TMA stencil
+// kernels also the padded fine-level copy and its tensor map
+agb_status build_f32(agb_elastic* h) {
+    const int nl = (int)h->L64.size();
+    if (h->L32.size() != h->L64.size()) TRY(alloc_levels32(h));
+    for (int l = 0; l < nl; l++) {
+        CK(launch_to_float(h->L64[l].C, h->L32[l].C, h->L64[l].G.N * h->nc, 1.0, h->stream));
+        CK(launch_diagonal<float>(h->sym, h->L32[l].C, h->L32[l].G, h->bc, h->L32[l].diag, h->stream));
+        h->launches += 2;
+    }
+    const LevelGeom<float>& G = h->L32[0].G;
+    if (h->opts.fine_kernel == 0 && zmarch_tma_supported(G.nx, G.ny, G.nz)) {
+        if (!h->c32pad) {
+            const size_t bytes = sizeof(float) * h->nc * (size_t)G.nz * G.ny * zmarch_tma_pitch(G.nx);
+            if (cudaMalloc(&h->c32pad, bytes) != cudaSuccess) {
+                h->c32pad = nullptr;
+                cudaGetLastError();
+                return fail(AGB_OUT_OF_MEMORY, "allocation of the padded FP32 stiffness failed");
+            }
+            h->have_cmap = false;
+        }
+        CK(launch_pad_stiffness(h->L32[0].C, h->c32pad, G.nx, G.ny, G.nz, h->nc, h->stream));
+        h->launches++;
+        if (!h->have_cmap) {
+            CK(make_stiffness_map(h->c32pad, G.nx, G.ny, G.nz, h->nc, &h->cmap));
+            h->have_cmap = true;
+        }
+    } else if (h->c32pad) {
+        free_pad(h);
+    }
+    h->have_f32 = true;
+    return AGB_OK;
+}
+
 agb_status prepare(agb_elastic* h) {
     if (h->prepared) return AGB_OK;
     if (!h->model_set) return fail(AGB_NOT_READY, "model not set (agb_elastic_set_model)");
@@ -316,15 +362,7 @@ agb_status prepare(agb_elastic* h) {
     }
     h->bot_dense = false;
     if (h->opts.bottom_solver == AGB_BOTTOM_DIRECT) TRY(build_bottom_dense(h));
-    if (h->opts.precision == AGB_PRECISION_MIXED) {
-        if (h->L32.size() != h->L64.size()) TRY(alloc_levels32(h));
-        for (int l = 0; l < nl; l++) {
-            CK(launch_to_float(h->L64[l].C, h->L32[l].C, h->L64[l].G.N * h->nc, 1.0, h->stream));
-            CK(launch_diagonal<float>(h->sym, h->L32[l].C, h->L32[l].G, h->bc, h->L32[l].diag, h->stream));
-            h->launches += 2;
-        }
-        h->have_f32 = true;
-    }
+    if (h->opts.precision == AGB_PRECISION_MIXED) TRY(build_f32(h));
     CK(cudaStreamSynchronize(h->stream));
     h->prepared = true;
     return AGB_OK;
@@ -333,15 +371,8 @@ agb_status prepare(agb_elastic* h) {
 agb_status ensure_f32(agb_elastic* h) {
     TRY(prepare(h));
     if (h->have_f32) return AGB_OK;
-    const int nl = (int)h->L64.size();
-    if (h->L32.size() != h->L64.size()) TRY(alloc_levels32(h));
-    for (int l = 0; l < nl; l++) {
-        CK(launch_to_float(h->L64[l].C, h->L32[l].C, h->L64[l].G.N * h->nc, 1.0, h->stream));
-        CK(launch_diagonal<float>(h->sym, h->L32[l].C, h->L32[l].G, h->bc, h->L32[l].diag, h->stream));
-        h->launches += 2;
-    }
+    TRY(build_f32(h));
     CK(cudaStreamSynchronize(h->stream));
-    h->have_f32 = true;
     return AGB_OK;
 }
 
@@ -354,11 +385,33 @@ template <>
 struct Fam<float> { enum { J = AGB_K_JACOBI_F32, R = AGB_K_RESIDUAL_F32 }; };
 
 // the z-marching kernels serve the FP32 fine level (FP64 stays on the
-// per-node kernels: it is FP64-pipe bound and the z-march form spills)
+// per-node kernels: it is FP64-pipe bound and the z-march form spills):
+// fine_kernel 0 the TMA-staged kernels where the grid allows, else the
+// register-staged ones; 2 always the register-staged ones
 template <typename T>
 bool use_zm(const agb_elastic*, int) { return false; }
 template <>
-bool use_zm<float>(const agb_elastic* h, int l) { return l == 0 && h->opts.fine_kernel == 0; }
+bool use_zm<float>(const agb_elastic* h, int l) { return l == 0 && h->opts.fine_kernel != 1; }
+
+// FP32 fine-level stencil: mode 0 out = A x, 1 one Jacobi sweep, 2 residual
+template <typename T>
+cudaError_t fine_zm(agb_elastic* h, int mode, const T* x, const T* C, const LevelGeom<T>& G, const T* b, const T* dg,
+                    T omega, T* out);
+template <>
+cudaError_t fine_zm<float>(agb_elastic* h, int mode, const float* x, const float* C, const LevelGeom<float>& G,
+                           const float* b, const float* dg, float omega, float* out) {
+    if (h->have_cmap && h->opts.fine_kernel == 0) {
+        h->launches++;  // interior + faces
+        return launch_zmarch_tma(mode, h->sym, h->cmap, x, C, G, h->bc, b, dg, omega, out, h->bottom_info + 3,
+                                 h->stream);
+    }
+    return launch_zmarch<float>(mode, h->sym, x, C, G, h->bc, b, dg, omega, out, h->stream);
+}
+template <>
+cudaError_t fine_zm<double>(agb_elastic* h, int mode, const double* x, const double* C, const LevelGeom<double>& G,
+                            const double* b, const double* dg, double omega, double* out) {
+    return launch_zmarch<double>(mode, h->sym, x, C, G, h->bc, b, dg, omega, out, h->stream);
+}
 
 // ncalls Fsmooth calls (2 sweeps each) on level l; cor_zero: cor is known 0
 template <typename T>
@@ -374,7 +427,7 @@ agb_status smooth(agb_elastic* h, std::vector<Lev<T>>& L, int l, int ncalls, boo
         {
             ProfScope ps(h, Fam<T>::J, l == 0 && !(cor_zero && s == 0));
             if (use_zm<T>(h, l) && !(cor_zero && s == 0))
-                CK(launch_zmarch<T>(1, h->sym, v.cor, v.C, v.G, h->bc, v.res, v.diag, w, v.tmp, h->stream));
+                CK(fine_zm<T>(h, 1, v.cor, v.C, v.G, v.res, v.diag, w, v.tmp));
             else
                 CK(launch_jacobi<T>(h->sym, (cor_zero && s == 0) ? nullptr : v.cor, v.res, v.diag, v.C, v.G, h->bc,
                                     w, v.tmp, h->stream));
@@ -435,7 +488,7 @@ agb_status vcycle(agb_elastic* h, std::vector<Lev<T>>& L) {
         {
             ProfScope ps(h, Fam<T>::R, l == 0);
             if (use_zm<T>(h, l))
-                CK(launch_zmarch<T>(2, h->sym, v.cor, v.C, v.G, h->bc, v.res, nullptr, T(0), v.rescor, h->stream));
+                CK(fine_zm<T>(h, 2, v.cor, v.C, v.G, v.res, nullptr, T(0), v.rescor));
             else
                 CK(launch_residual<T>(h->sym, v.cor, v.res, v.C, v.G, h->bc, v.rescor, nullptr, nullptr, h->stream));
         }
@@ -551,27 +604,43 @@ agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, doub
     int j = 0;
     double resid = beta;
     for (; j < m; j++) {
-        // Z_j = M^-1 V_j (one V-cycle on the correction equation)
-        CK(cudaMemcpyAsync(top.res, K.V[j], sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
-        TRY(vcycle<T>(h, L));
-        CK(cudaMemcpyAsync(K.Z[j], top.cor, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
+        // Z_j = M^-1 V_j (one V-cycle on the correction equation).  The
+        // cycle reads the fine right-hand side in place and builds the fine
+        // correction in Z_j directly (the smoother ping-pongs cor and tmp, so
+        // an odd sweep count leaves it in the other buffer: copied back).
+        {
+            T* res0 = top.res;
+            T* cor0 = top.cor;
+            T* tmp0 = top.tmp;
+            top.res = K.V[j];
+            top.cor = K.Z[j];
+            const agb_status vs = vcycle<T>(h, L);
+            T* out = top.cor;
+            top.res = res0;
+            top.cor = cor0;
+            top.tmp = tmp0;
+            TRY(vs);
+            if (out != K.Z[j]) CK(cudaMemcpyAsync(K.Z[j], out, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
+        }
         // w = A Z_j
         if (use_zm<T>(h, 0))
-            CK(launch_zmarch<T>(0, h->sym, K.Z[j], top.C, top.G, h->bc, nullptr, nullptr, T(0), K.w, st));
+            CK(fine_zm<T>(h, 0, K.Z[j], top.C, top.G, nullptr, nullptr, T(0), K.w));
         else
             CK(launch_fapply<T>(h->sym, K.Z[j], top.C, top.G, h->bc, K.w, st));
         // classical Gram-Schmidt, re-orthogonalised once unless krylov_reorth = 0
-        CK(launch_multidot<T>(K.Vdev, j + 1, K.w, n, K.part, K.dots, st));
-        CK(launch_multiaxpy<T>(K.w, 1.0, K.Vdev, K.dots, -1.0, j + 1, n, st));
+        // (the last projection also leaves ||w||^2 in dots[80])
         const bool reorth = h->opts.krylov_reorth != 0;
+        CK(launch_multidot<T>(K.Vdev, j + 1, K.w, n, K.part, K.dots, st));
         if (reorth) {
+            CK(launch_multiaxpy<T>(K.w, 1.0, K.Vdev, K.dots, -1.0, j + 1, n, st));
             CK(launch_multidot<T>(K.Vdev, j + 1, K.w, n, K.part, K.dots + 40, st));
-            CK(launch_multiaxpy<T>(K.w, 1.0, K.Vdev, K.dots + 40, -1.0, j + 1, n, st));
+            CK(launch_multiaxpy_norm<T>(K.w, 1.0, K.Vdev, K.dots + 40, -1.0, j + 1, n, K.part, K.dots + 80, st));
+        } else {
+            CK(launch_multiaxpy_norm<T>(K.w, 1.0, K.Vdev, K.dots, -1.0, j + 1, n, K.part, K.dots + 80, st));
         }
-        CK(launch_multidot<T>(K.Wdev, 1, K.w, n, K.part, K.dots + 80, st));
         CK(cudaMemcpyAsync(K.hdots, K.dots, sizeof(double) * 120, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        h->launches += reorth ? 12 : 8;
+        h->launches += reorth ? 8 : 5;
         for (int i = 0; i <= j; i++) H[(size_t)i * m + j] = K.hdots[i] + (reorth ? K.hdots[40 + i] : 0.0);
         const double hn = std::sqrt(std::max(K.hdots[80], 0.0));
         H[(size_t)(j + 1) * m + j] = hn;
@@ -690,10 +759,15 @@ agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_re
         }
         if (fixed && status != AGB_NAN) status = AGB_OK;
     }
-    int binfo[2] = {0, 0};
-    CK(cudaMemcpyAsync(h->norms_host, h->bottom_info, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    int binfo[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(h->norms_host, h->bottom_info, 4 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    std::memcpy(binfo, h->norms_host, 2 * sizeof(int));
+    std::memcpy(binfo, h->norms_host, 4 * sizeof(int));
+    if (binfo[3] != 0) {
+        CK(cudaMemsetAsync(h->bottom_info + 3, 0, sizeof(int), h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        return fail(AGB_CUDA_ERROR, "a TMA load of the fine-level stencil kernel did not complete in time");
+    }
     prof_collect(h);
     if (rep) {
         rep->status = status;
@@ -788,6 +862,7 @@ static agb_status check_opts(const agb_solver_opts* o) {
     if (o->solver != AGB_SOLVER_VCYCLE && o->solver != AGB_SOLVER_FGMRES) return fail(AGB_BAD_ARG, "unknown solver");
     if (o->bottom_solver < AGB_BOTTOM_BICGSTAB || o->bottom_solver > AGB_BOTTOM_SMOOTHER)
         return fail(AGB_BAD_ARG, "unknown bottom solver");
+    if (o->fine_kernel < 0 || o->fine_kernel > 2) return fail(AGB_BAD_ARG, "fine_kernel must be 0, 1 or 2");
     if (o->solver == AGB_SOLVER_FGMRES && (o->krylov_dim < 1 || o->krylov_dim > 39))
         return fail(AGB_BAD_ARG, "krylov_dim must lie in [1, 39]");
     if (o->solver == AGB_SOLVER_FGMRES && !(o->inner_tol > 0.0 && o->inner_tol < 1.0))
@@ -838,6 +913,7 @@ agb_status agb_elastic_destroy(agb_elastic* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     free_levels(h->L64);
     free_levels(h->L32);
+    free_pad(h);
     cudaFree(h->partials);
     cudaFree(h->norms_dev);
     if (h->norms_host) cudaFreeHost(h->norms_host);
@@ -870,6 +946,7 @@ agb_status agb_elastic_set_opts(agb_elastic* h, const agb_solver_opts* o) {
             CK(cudaStreamSynchronize(h->stream));
         }
         free_levels(h->L32);
+        free_pad(h);
         h->have_f32 = false;
         agb_status st = alloc_levels64(h);
         if (st == AGB_OK && keep)
@@ -991,8 +1068,7 @@ agb_status agb_elastic_fapply_f32(agb_elastic* h, int level, const float* u, flo
     {
         ProfScope ps(h, AGB_K_FAPPLY_F32, level == 0);
         if (use_zm<float>(h, level))
-            CK(launch_zmarch<float>(0, h->sym, (const float*)du, v.C, v.G, h->bc, nullptr, nullptr, 0.f, (float*)df,
-                                    h->stream));
+            CK(fine_zm<float>(h, 0, (const float*)du, v.C, v.G, nullptr, nullptr, 0.f, (float*)df));
         else
             CK(launch_fapply<float>(h->sym, (const float*)du, v.C, v.G, h->bc, (float*)df, h->stream));
     }

@@ -568,38 +568,133 @@ cudaError_t launch_stress_strain(int sym, const double* u, const double* F0, int
 namespace agb {
 
 // ---------------------------------------------------------------- Krylov
-// out[i] = sum_q V_i[q] * w[q] for i < k (FP64 accumulation), two passes:
-// per-block partial sums, then one block per i over the partials.  Blocks
-// are organised as (element range) x (chunk of 8 vectors) so the 8
-// accumulators of a thread stay in registers.
+// Sum of products in the vectors' own type.  For FP32 the products' rounding
+// errors (exact through an FMA) and the additions' errors (TwoSum, Knuth) are
+// carried in a second FP32 word, so the result is about as accurate as FP64
+// accumulation while every operation runs on the FP32 pipe.
+template <typename T>
+struct Acc {
+    T s = T(0);
+    __device__ __forceinline__ void add(T a, T b) { s = fma(a, b, s); }
+    __device__ __forceinline__ T value() const { return s; }
+    __device__ __forceinline__ double dvalue() const { return (double)s; }
+};
+template <>
+struct Acc<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float a, float b) {
+        const float p = a * b;
+        const float pe = fmaf(a, b, -p);
+        const float t = s + p;
+        const float z = t - s;
+        const float e = (s - (t - z)) + (p - z);
+        s = t;
+        c += e + pe;
+    }
+    __device__ __forceinline__ float value() const { return s + c; }
+    __device__ __forceinline__ double dvalue() const { return (double)s + (double)c; }
+};
+
+// 16-byte vector view of a T array: float4 / double2.  Every Krylov vector
+// is its own cudaMalloc allocation, so its base is 16-byte aligned; the
+// n % W tail is handled element by element.
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using V = float4;
+    static constexpr int W = 4;
+    __device__ static __forceinline__ float get(const float4& v, int c) {
+        return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
+    }
+    __device__ static __forceinline__ void set(float4& v, int c, float x) {
+        if (c == 0) v.x = x; else if (c == 1) v.y = x; else if (c == 2) v.z = x; else v.w = x;
+    }
+};
+template <>
+struct Vec16<double> {
+    using V = double2;
+    static constexpr int W = 2;
+    __device__ static __forceinline__ double get(const double2& v, int c) { return c == 0 ? v.x : v.y; }
+    __device__ static __forceinline__ void set(double2& v, int c, double x) {
+        if (c == 0) v.x = x; else v.y = x;
+    }
+};
+
+// Block sum of one double per thread into part[blockIdx.x * KMAX + col].
 static constexpr int KMAX = 40;
+__device__ __forceinline__ void block_sum_to(double v, double* part, int col) {
+    __shared__ double sh[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[q];
+        part[(int64_t)blockIdx.x * KMAX + col] = t;
+    }
+}
+
+// out[i] = sum_q V_i[q] * w[q] for i < k, two passes: per-block partial sums,
+// then one block per i over the partials.  Blocks are organised as (element
+// range) x (chunk of 8 vectors) so the 8 accumulators of a thread stay in
+// registers.  Each thread streams 16-byte loads of two element groups per
+// iteration, which keeps (k+1) x 1 KB in flight per warp: the loads, not
+// the arithmetic, set the pace.
 static constexpr int KCH = 8;
 
-// Per-thread sums run in the vectors' own type (FP32 vectors: FP32 FMA, the
-// 1/64-rate FP64 pipe of GB300 would bound the kernel); the cross-thread
-// and cross-block reductions run in FP64.
+// Per-thread sums run in the vectors' own type (FP32 vectors: compensated
+// FP32, the 1/64-rate FP64 pipe of GB300 would bound the kernel); the
+// cross-thread and cross-block reductions run in FP64.
 template <typename T>
-__global__ void __launch_bounds__(256) k_multidot_partial(const T* const* __restrict__ V, int k, const T* __restrict__ w,
-                                                          int64_t n, double* __restrict__ part) {
+__global__ void __launch_bounds__(256, 4) k_multidot_partial(const T* const* __restrict__ V, int k,
+                                                             const T* __restrict__ w, int64_t n,
+                                                             double* __restrict__ part) {
+    using VT = Vec16<T>;
+    using V4 = typename VT::V;
+    constexpr int W = VT::W;
     const int c0 = blockIdx.y * KCH;
-    __shared__ const T* vp[KCH];
-    if (threadIdx.x < KCH) vp[threadIdx.x] = (c0 + (int)threadIdx.x < k) ? V[c0 + threadIdx.x] : nullptr;
-    __syncthreads();
     const int kk = min(KCH, k - c0);
-    T acc[KCH];
+    const V4* vp[KCH];
 #pragma unroll
-    for (int i = 0; i < KCH; i++) acc[i] = T(0);
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    for (int i = 0; i < KCH; i++) vp[i] = reinterpret_cast<const V4*>(i < kk ? V[c0 + i] : V[c0]);
+    const V4* w4 = reinterpret_cast<const V4*>(w);
+    Acc<T> acc[KCH];
+    const int64_t n4 = n / W;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4; q += 2 * stride) {
+        const int64_t q2 = q + stride;
+        const bool two = q2 < n4;
+        const V4 wa = w4[q];
+        V4 wb = wa;
+        if (two) wb = w4[q2];
+#pragma unroll
+        for (int i = 0; i < KCH; i++) {
+            if (i < kk) {
+                const V4 va = vp[i][q];
+#pragma unroll
+                for (int c = 0; c < W; c++) acc[i].add(VT::get(va, c), VT::get(wa, c));
+                if (two) {
+                    const V4 vb = vp[i][q2];
+#pragma unroll
+                    for (int c = 0; c < W; c++) acc[i].add(VT::get(vb, c), VT::get(wb, c));
+                }
+            }
+        }
+    }
+    // tail elements n4*W .. n-1
+    for (int64_t q = n4 * W + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += stride) {
         const T wq = w[q];
 #pragma unroll
         for (int i = 0; i < KCH; i++)
-            if (i < kk) acc[i] += vp[i][q] * wq;
+            if (i < kk) acc[i].add(V[c0 + i][q], wq);
     }
     __shared__ double sh[8][KCH];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < KCH; i++) {
-        double v = (double)acc[i];
+        double v = acc[i].dvalue();
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) sh[wid][i] = v;
@@ -645,51 +740,108 @@ template cudaError_t launch_multidot<double>(const double* const*, int, const do
 template cudaError_t launch_multidot<float>(const float* const*, int, const float*, int64_t, double*, double*,
                                             cudaStream_t);
 
-// w = beta * w + sum_i coef[i] * scale * V_i  (coef in device memory); two
-// elements per thread, pointer table and coefficients in shared memory,
-// arithmetic in the vectors' type
+// w = beta * w + sum_i coef[i] * scale * V_i  (coef in device memory), one
+// 16-byte group per thread and step, the loop over the vectors unrolled by 4
+// so four loads are in flight; coefficients and the pointer table in shared
+// memory, compensated arithmetic in the vectors' type.  With part non-null
+// the block sums of w_new^2 go to part[blockIdx.x * KMAX] (the norm of the
+// result without another pass over it).
 template <typename T>
-__global__ void __launch_bounds__(256) k_multiaxpy(T* __restrict__ w, double beta, const T* const* __restrict__ V,
-                                                   const double* __restrict__ coef, double scale, int k, int64_t n) {
+__global__ void __launch_bounds__(256, 4) k_multiaxpy(T* __restrict__ w, double beta, const T* const* __restrict__ V,
+                                                      const double* __restrict__ coef, double scale, int k, int64_t n,
+                                                      double* __restrict__ part) {
+    using VT = Vec16<T>;
+    using V4 = typename VT::V;
+    constexpr int W = VT::W;
     __shared__ T c[KMAX];
-    __shared__ const T* vp[KMAX];
-    for (int i = threadIdx.x; i < k; i += blockDim.x) { c[i] = (T)(coef[i] * scale); vp[i] = V[i]; }
+    __shared__ const V4* vp[KMAX];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+        c[i] = (T)(coef[i] * scale);
+        vp[i] = reinterpret_cast<const V4*>(V[i]);
+    }
     __syncthreads();
     const T bt = (T)beta;
+    V4* w4 = reinterpret_cast<V4*>(w);
+    const int64_t n4 = n / W;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += 2 * stride) {
-        const int64_t q2 = q + stride;
-        const bool two = q2 < n;
-        T a0 = (beta == 0.0) ? T(0) : bt * w[q];
-        T a1 = (two && beta != 0.0) ? bt * w[q2] : T(0);
-        for (int i = 0; i < k; i++) {
-            const T* v = vp[i];
-            const T ci = c[i];
-            a0 += ci * v[q];
-            if (two) a1 += ci * v[q2];
+    Acc<T> nrm;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4; q += stride) {
+        Acc<T> a[W];
+        if (beta != 0.0) {
+            const V4 x = w4[q];
+#pragma unroll
+            for (int e = 0; e < W; e++) a[e].add(bt, VT::get(x, e));
         }
-        w[q] = a0;
-        if (two) w[q2] = a1;
+#pragma unroll 4
+        for (int i = 0; i < k; i++) {
+            const V4 v = vp[i][q];
+            const T ci = c[i];
+#pragma unroll
+            for (int e = 0; e < W; e++) a[e].add(ci, VT::get(v, e));
+        }
+        V4 o;
+#pragma unroll
+        for (int e = 0; e < W; e++) {
+            const T r = a[e].value();
+            VT::set(o, e, r);
+            nrm.add(r, r);
+        }
+        w4[q] = o;
     }
+    for (int64_t q = n4 * W + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += stride) {
+        Acc<T> a;
+        if (beta != 0.0) a.add(bt, w[q]);
+        for (int i = 0; i < k; i++) a.add(c[i], V[i][q]);
+        const T r = a.value();
+        w[q] = r;
+        nrm.add(r, r);
+    }
+    if (part) block_sum_to(nrm.dvalue(), part, 0);
 }
 
 template <typename T>
 cudaError_t launch_multiaxpy(T* w, double beta, const T* const* V, const double* coef, double scale, int k, int64_t n,
                              cudaStream_t s) {
     if (k < 0 || k > KMAX) return cudaErrorInvalidValue;
-    k_multiaxpy<T><<<flat_blocks(n), 256, 0, s>>>(w, beta, V, coef, scale, k, n);
+    k_multiaxpy<T><<<multidot_blocks(), 256, 0, s>>>(w, beta, V, coef, scale, k, n, nullptr);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_multiaxpy_norm(T* w, double beta, const T* const* V, const double* coef, double scale, int k,
+                                  int64_t n, double* part, double* norm2, cudaStream_t s) {
+    if (k < 0 || k > KMAX) return cudaErrorInvalidValue;
+    const int nb = multidot_blocks();
+    k_multiaxpy<T><<<nb, 256, 0, s>>>(w, beta, V, coef, scale, k, n, part);
+    k_multidot_final<<<1, 256, 0, s>>>(part, nb, 1, norm2);
     return cudaGetLastError();
 }
 template cudaError_t launch_multiaxpy<double>(double*, double, const double* const*, const double*, double, int,
                                               int64_t, cudaStream_t);
 template cudaError_t launch_multiaxpy<float>(float*, double, const float* const*, const double*, double, int, int64_t,
                                              cudaStream_t);
+template cudaError_t launch_multiaxpy_norm<double>(double*, double, const double* const*, const double*, double, int,
+                                                   int64_t, double*, double*, cudaStream_t);
+template cudaError_t launch_multiaxpy_norm<float>(float*, double, const float* const*, const double*, double, int,
+                                                  int64_t, double*, double*, cudaStream_t);
 
-// dst = a * src
+// dst = a * src, 16-byte groups (both arrays are cudaMalloc bases)
 template <typename T>
-__global__ void k_scale_copy(const T* __restrict__ src, T* __restrict__ dst, double a, int64_t n) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-        dst[q] = (T)(a * (double)src[q]);
+__global__ void __launch_bounds__(256) k_scale_copy(const T* __restrict__ src, T* __restrict__ dst, double a,
+                                                    int64_t n) {
+    using VT = Vec16<T>;
+    using V4 = typename VT::V;
+    constexpr int W = VT::W;
+    const int64_t n4 = n / W;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const T at = (T)a;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4; q += stride) {
+        const V4 v = reinterpret_cast<const V4*>(src)[q];
+        V4 o;
+#pragma unroll
+        for (int e = 0; e < W; e++) VT::set(o, e, at * VT::get(v, e));
+        reinterpret_cast<V4*>(dst)[q] = o;
+    }
+    for (int64_t q = n4 * W + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += stride) dst[q] = at * src[q];
 }
 template <typename T>
 cudaError_t launch_scale_copy(const T* src, T* dst, int64_t n, double a, cudaStream_t s) {

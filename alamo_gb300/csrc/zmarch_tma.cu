@@ -1,0 +1,415 @@
+// FP32 fine-level stencil kernels with the stiffness staged by TMA.
+//
+// Interior nodes (1..n-2 on every axis) are computed by a z-marching 32 x 8
+// thread block; the six boundary faces by a separate per-node kernel, so the
+// marching tiles start at node 1 and the 255 interior columns of a 257-node
+// axis fill 8 tiles of 32 exactly.
+//
+// Per z-plane a block needs
+//   * the displacement of planes k-1, k, k+1 with a one-node x/y halo
+//     (3 x 10 x 34 values): a 4-slot ring filled by 4-byte cp.async, plane
+//     k+2 issued at the top of step k;
+//   * the stiffness of plane k with the x/y halo (for the in-plane
+//     derivatives of C) and of plane k+1 at the block's own columns (for
+//     the z-derivative): a 3-slot ring of TMA boxes (36 x 10 nodes x NC
+//     entries), plane k+2 issued at the top of step k into the slot plane
+//     k-1 has left; the stiffness of plane k-1 at the own column is kept in
+//     registers from the previous step.
+// Everything the stencil reads then comes from shared memory at offsets that
+// are compile-time constants, and each array is read from HBM about once per
+// sweep.  The TMA box starts at x = x0 - 1 = 32 * blockIdx.x, a multiple of
+// 4 floats (16 bytes); the stiffness copy it reads has its x pitch padded to
+// a multiple of 4 floats so every global stride is a multiple of 16 bytes.
+//
+// Every wait on an mbarrier is bounded: after the limit the block records
+// the failure in *err, stops marching (uniformly, through a shared flag),
+// waits (bounded) for its TMA copies still in flight and returns.
+//
+// Epilogues: FAPPLY out = A x; JACOBI one damped-Jacobi sweep; RESIDUAL
+// out = b - A x.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "agb_launch.h"
+#include "operator.cuh"
+#include "zmarch_tma.h"
+
+namespace agb {
+
+namespace {
+
+constexpr int TX = 32, TY = 8, NT = TX * TY;
+constexpr int UHX = TX + 2, UHY = TY + 2;
+constexpr int UPL = 3 * UHY * UHX;                // displacement values per staged plane
+constexpr int US = 4;                             // displacement ring slots
+constexpr int U_PER_T = (UPL + NT - 1) / NT;      // cp.async per thread per plane
+constexpr int CBX = 36, CBY = 10;                 // TMA box (x, y) of a stiffness plane
+constexpr int CEL = CBX * CBY;                    // floats per stiffness entry in a slot
+constexpr int CS = 3;                             // stiffness ring slots
+constexpr uint64_t WAIT_NS = 1000000000ull;       // 1 s: a TMA load takes microseconds
+
+template <int NC>
+struct ZtSmem {
+    static constexpr int slot_bytes = ((NC * CEL * 4 + 127) / 128) * 128;
+    static constexpr int c_bytes = CS * slot_bytes;
+    static constexpr int u_bytes = US * UPL * 4;
+    static constexpr int bar_off = c_bytes + u_bytes;
+    static constexpr int total = bar_off + CS * 8 + 128;  // + alignment slack
+    static constexpr uint32_t box_bytes = NC * CEL * 4;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// true once the phase of the given parity has completed; false when it has
+// not completed within WAIT_NS (each try_wait returns after at most a short
+// hardware time limit, so the loop ends)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    uint64_t t0 = 0;
+    for (int it = 0;; it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (it == 0) t0 = global_ns();
+        else if (global_ns() - t0 > WAIT_NS) return false;
+    }
+}
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, int e,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(e), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void cp_async4(uint32_t dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <int SYM, int MODE>
+__global__ void __launch_bounds__(NT, 2)
+    k_zmarch_tma(const __grid_constant__ CUtensorMap cmap, const float* __restrict__ x, LevelGeom<float> G,
+                 const float* __restrict__ b, const float* __restrict__ dg, float omega, float* __restrict__ out,
+                 int kchunk, int* __restrict__ err) {
+    constexpr int NC = SYM == SYM_ISO ? 2 : 21;
+    using SM = ZtSmem<NC>;
+    extern __shared__ unsigned char zt_raw[];
+    __shared__ int abort_flag;
+    const uint32_t raw = smem_u32(zt_raw);
+    const uint32_t pad = ((raw + 127u) & ~127u) - raw;
+    unsigned char* sm = zt_raw + pad;
+    float* Cs = reinterpret_cast<float*>(sm);
+    float* Us = reinterpret_cast<float*>(sm + SM::c_bytes);
+    const uint32_t cs_u32 = raw + pad;
+    const uint32_t us_u32 = cs_u32 + SM::c_bytes;
+    const uint32_t bar_u32 = cs_u32 + SM::bar_off;
+
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int x0 = 1 + blockIdx.x * TX, y0 = 1 + blockIdx.y * TY;
+    const int k0 = 1 + blockIdx.z * kchunk;
+    const int k1 = min(k0 + kchunk, G.nz - 1);
+    const int i = x0 + tx, j = y0 + ty;
+    const bool col = (i <= G.nx - 2) & (j <= G.ny - 2);
+    const int64_t N = G.N, sy = G.sy, sz = G.sz;
+
+    // this thread's share of a staged displacement plane
+    int soff[U_PER_T];
+    int64_t goff[U_PER_T];
+    bool gval[U_PER_T];
+#pragma unroll
+    for (int r = 0; r < U_PER_T; r++) {
+        const int q = tid + r * NT;
+        const int p = q / (UHY * UHX), rem = q - p * (UHY * UHX), yy = rem / UHX, xx = rem - yy * UHX;
+        const int gx = x0 - 1 + xx, gy = y0 - 1 + yy;
+        soff[r] = q;
+        gval[r] = (q < UPL) & (gx < G.nx) & (gy < G.ny);
+        goff[r] = p * N + gx + sy * gy;
+    }
+    auto issue_u = [&](int kk) {
+        const uint32_t dst = us_u32 + (uint32_t)((kk % US) * UPL) * 4u;
+#pragma unroll
+        for (int r = 0; r < U_PER_T; r++)
+            if (gval[r]) cp_async4(dst + soff[r] * 4u, x + goff[r] + sz * (int64_t)kk);
+        cp_async_commit();
+    };
+    auto issue_c = [&](int kk) {  // one thread
+        const int s = kk % CS;
+        mbar_expect_tx(bar_u32 + 8u * s, SM::box_bytes);
+        tma_load_4d(cs_u32 + (uint32_t)(s * SM::slot_bytes), &cmap, TX * blockIdx.x, TY * blockIdx.y, kk, 0,
+                    bar_u32 + 8u * s);
+    };
+    // plane kk is the n-th load into its slot, n = (kk - (k0 - 1)) / CS
+    auto parity = [&](int kk) { return (uint32_t)(((kk - (k0 - 1)) / CS) & 1); };
+    auto cslot = [&](int kk) { return Cs + (kk % CS) * (SM::slot_bytes / 4) + (ty + 1) * CBX + (tx + 1); };
+
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int s = 0; s < CS; s++) mbar_init(bar_u32 + 8u * s, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    int issued = k0 + 1;  // last plane issued (thread 0 uses it on abort)
+    if (tid == 0) {
+        issue_c(k0 - 1);
+        issue_c(k0);
+        issue_c(k0 + 1);
+    }
+    issue_u(k0 - 1);
+    issue_u(k0);
+    issue_u(k0 + 1);
+
+    float Cp[NC];
+    bool ok = mbar_wait(bar_u32 + 8u * ((k0 - 1) % CS), parity(k0 - 1));
+    ok = ok && mbar_wait(bar_u32 + 8u * (k0 % CS), parity(k0));
+    {
+        const float* c = cslot(k0 - 1);
+#pragma unroll
+        for (int e = 0; e < NC; e++) Cp[e] = c[e * CEL];
+    }
+    if (!ok) {
+        abort_flag = 1;
+        if (err) atomicExch(err, 1);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+
+    for (int k = k0; k < k1 && !abort_flag; k++) {
+        if (k + 2 <= k1) {
+            if (tid == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue_c(k + 2);
+            }
+            issue_u(k + 2);
+            issued = k + 2;
+        }
+        const int64_t id = i + sy * j + sz * (int64_t)k;
+        float bq[3] = {0.f, 0.f, 0.f}, dq[3] = {1.f, 1.f, 1.f};
+        if (col) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                if (MODE >= 1) bq[c] = b[c * N + id];
+                if (MODE == 1) dq[c] = dg[c * N + id];
+            }
+        }
+        const bool okn = mbar_wait(bar_u32 + 8u * ((k + 1) % CS), parity(k + 1));
+        const float* cc = cslot(k);
+        if (col && okn) {
+            const float* cn = cslot(k + 1);
+            const float* u0 = Us + (k % US) * UPL + (ty + 1) * UHX + (tx + 1);
+            const float* um = Us + ((k + US - 1) % US) * UPL + (ty + 1) * UHX + (tx + 1);
+            const float* up = Us + ((k + 1) % US) * UPL + (ty + 1) * UHX + (tx + 1);
+            auto U = [&](int p, int a, int bb, int c) -> float {
+                const float* s = c == 0 ? u0 : (c < 0 ? um : up);
+                return s[p * (UHY * UHX) + bb * UHX + a];
+            };
+            auto Cf = [&](int e, int a, int bb, int c) -> float {
+                if (c > 0) return cn[e * CEL];
+                if (c < 0) return Cp[e];
+                return cc[e * CEL + bb * CBX + a];
+            };
+            float r[3];
+            interior_rows<float, SYM>(U, Cf, G, r);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const int64_t q = c * N + id;
+                if (MODE == 0) {
+                    out[q] = r[c];
+                } else if (MODE == 1) {
+                    const float xv = u0[c * (UHY * UHX)];
+                    const float rx = r[c] - xv * dq[c];
+                    out[q] = (1.f - omega) * xv + omega * (bq[c] - rx) / dq[c];
+                } else {
+                    out[q] = bq[c] - r[c];
+                }
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < NC; e++) Cp[e] = cc[e * CEL];
+        if (!okn) {
+            abort_flag = 1;
+            if (err) atomicExch(err, 1);
+        }
+        cp_async_wait_all();
+        __syncthreads();
+    }
+    if (abort_flag && tid == 0) {
+        // bounded wait for the TMA loads still in flight (at most the
+        // latest load of each slot) before the block gives its shared
+        // memory back
+        for (int kk = max(issued - (CS - 1), k0 - 1); kk <= issued; kk++)
+            mbar_wait(bar_u32 + 8u * (kk % CS), parity(kk));
+    }
+}
+
+// Boundary faces: one thread per face node, the general BC rows.
+__device__ __forceinline__ void face_node(int64_t t, int nx, int ny, int nz, int& i, int& j, int& k) {
+    const int64_t fz = (int64_t)nx * ny, fy = (int64_t)nx * (nz - 2);
+    if (t < 2 * fz) {
+        k = t < fz ? 0 : nz - 1;
+        const int64_t r = t < fz ? t : t - fz;
+        j = (int)(r / nx);
+        i = (int)(r - (int64_t)j * nx);
+        return;
+    }
+    t -= 2 * fz;
+    if (t < 2 * fy) {
+        j = t < fy ? 0 : ny - 1;
+        const int64_t r = t < fy ? t : t - fy;
+        k = 1 + (int)(r / nx);
+        i = (int)(r % nx);
+        return;
+    }
+    t -= 2 * fy;
+    const int64_t fx = (int64_t)(ny - 2) * (nz - 2);
+    i = t < fx ? 0 : nx - 1;
+    const int64_t r = t < fx ? t : t - fx;
+    k = 1 + (int)(r / (ny - 2));
+    j = 1 + (int)(r % (ny - 2));
+}
+
+template <int SYM, int MODE>
+__global__ void __launch_bounds__(256) k_zm_faces(const float* __restrict__ x, const float* __restrict__ C,
+                                                  LevelGeom<float> G, BcTable bc, const float* __restrict__ b,
+                                                  const float* __restrict__ dg, float omega, float* __restrict__ out,
+                                                  int64_t nfaces) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nfaces;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        face_node(t, G.nx, G.ny, G.nz, i, j, k);
+        const int64_t id = i + G.sy * j + G.sz * (int64_t)k, N = G.N;
+        auto cf = [&](int a) { return C[a * N + id]; };
+        float r[3];
+        apply_boundary<float, SYM>(x, G, bc, cf, i, j, k, id, r);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const int64_t q = c * N + id;
+            if (MODE == 0) {
+                out[q] = r[c];
+            } else if (MODE == 1) {
+                const float xv = x[q], d = dg[q];
+                out[q] = (1.f - omega) * xv + omega * (b[q] - (r[c] - xv * d)) / d;
+            } else {
+                out[q] = b[q] - r[c];
+            }
+        }
+    }
+}
+
+// FP32 stiffness, SoA (nc, nz, ny, nx) -> padded (nc, nz, ny, px), zero pad
+__global__ void k_pad_planes(const float* __restrict__ src, float* __restrict__ dst, int nx, int px, int64_t rows) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * px;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = t / px;
+        const int xx = (int)(t - row * px);
+        dst[t] = xx < nx ? src[row * nx + xx] : 0.f;
+    }
+}
+
+int zt_kchunk(int nz) { return nz >= 96 ? 32 : 16; }
+
+}  // namespace
+
+bool zmarch_tma_supported(int nx, int ny, int nz) {
+    // an interior on every axis; 32-bit TMA coordinates
+    return nx >= 3 && ny >= 3 && nz >= 3 && nx < (1 << 30) && ny < (1 << 30) && nz < (1 << 30);
+}
+
+int64_t zmarch_tma_pitch(int nx) { return (nx + 3) / 4 * 4; }
+
+cudaError_t make_stiffness_map(const float* Cpad, int nx, int ny, int nz, int nc, CUtensorMap* map) {
+    using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeFn encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorSymbolNotFound;
+        encode = reinterpret_cast<EncodeFn>(fn);
+    }
+    const int64_t px = zmarch_tma_pitch(nx);
+    const cuuint64_t dims[4] = {(cuuint64_t)px, (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)nc};
+    const cuuint64_t strides[3] = {(cuuint64_t)px * 4, (cuuint64_t)px * ny * 4, (cuuint64_t)px * ny * nz * 4};
+    const cuuint32_t box[4] = {(cuuint32_t)CBX, (cuuint32_t)CBY, 1u, (cuuint32_t)nc};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(Cpad), dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t launch_pad_stiffness(const float* C, float* Cpad, int nx, int ny, int nz, int nc, cudaStream_t s) {
+    const int64_t px = zmarch_tma_pitch(nx);
+    const int64_t rows = (int64_t)nc * nz * ny;
+    int64_t blocks = (rows * px + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_pad_planes<<<(int)blocks, 256, 0, s>>>(C, Cpad, nx, (int)px, rows);
+    return cudaGetLastError();
+}
+
+template <int SYM, int MODE>
+static cudaError_t zt_launch(const CUtensorMap& map, const float* x, const float* C, const LevelGeom<float>& G,
+                             const BcTable& bc, const float* b, const float* dg, float omega, float* out, int* err,
+                             cudaStream_t s) {
+    constexpr int NC = SYM == SYM_ISO ? 2 : 21;
+    constexpr int bytes = ZtSmem<NC>::total;
+    static bool configured[64] = {};  // the attribute is set once per device
+    int dev = 0;
+    cudaError_t e0 = cudaGetDevice(&dev);
+    if (e0 != cudaSuccess) return e0;
+    if (dev < 0 || dev >= 64 || !configured[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(k_zmarch_tma<SYM, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             bytes);
+        if (e != cudaSuccess) return e;
+        if (dev >= 0 && dev < 64) configured[dev] = true;
+    }
+    const int kc = zt_kchunk(G.nz);
+    const int ni = G.nx - 2, nj = G.ny - 2, nk = G.nz - 2;
+    dim3 blk(TX, TY, 1), grd((ni + TX - 1) / TX, (nj + TY - 1) / TY, (nk + kc - 1) / kc);
+    k_zmarch_tma<SYM, MODE><<<grd, blk, bytes, s>>>(map, x, G, b, dg, omega, out, kc, err);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int64_t nf = G.N - (int64_t)ni * nj * nk;
+    int64_t fb = (nf + 255) / 256;
+    if (fb > 152 * 8) fb = 152 * 8;
+    k_zm_faces<SYM, MODE><<<(int)fb, 256, 0, s>>>(x, C, G, bc, b, dg, omega, out, nf);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zmarch_tma(int mode, int sym, const CUtensorMap& map, const float* x, const float* C,
+                              const LevelGeom<float>& G, const BcTable& bc, const float* b, const float* dg,
+                              float omega, float* out, int* err, cudaStream_t s) {
+    if (!zmarch_tma_supported(G.nx, G.ny, G.nz)) return cudaErrorInvalidValue;
+    if (sym == SYM_ISO) {
+        if (mode == 0) return zt_launch<SYM_ISO, 0>(map, x, C, G, bc, b, dg, omega, out, err, s);
+        if (mode == 1) return zt_launch<SYM_ISO, 1>(map, x, C, G, bc, b, dg, omega, out, err, s);
+        return zt_launch<SYM_ISO, 2>(map, x, C, G, bc, b, dg, omega, out, err, s);
+    }
+    if (mode == 0) return zt_launch<SYM_MM, 0>(map, x, C, G, bc, b, dg, omega, out, err, s);
+    if (mode == 1) return zt_launch<SYM_MM, 1>(map, x, C, G, bc, b, dg, omega, out, err, s);
+    return zt_launch<SYM_MM, 2>(map, x, C, G, bc, b, dg, omega, out, err, s);
+}
+
+}  // namespace agb

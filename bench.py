@@ -156,8 +156,8 @@ def measured_peaks():
 # --------------------------------------------------------------- CPU sample
 def cpu_sample(cfg, n_override, C, F0, bc, dx, cycles):
     """Oracle (the reference's CPU path restated) on all host threads: time
-    the set-up plus two fixed V-cycles and one fixed V-cycle, scale to the
-    FP64 cycle count of the whole solve."""
+    the right-hand side, the hierarchy set-up and two fixed V-cycles, and
+    scale the per-cycle time to the FP64 cycle count of the whole solve."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
@@ -170,20 +170,17 @@ def cpu_sample(cfg, n_override, C, F0, bc, dx, cycles):
     b = O.bc_init(u, bt, bv)
     rhs = O.build_rhs(C, F0, bt, u, b, dx)
     t_rhs = time.perf_counter() - t0
-    t1 = time.perf_counter()
-    O.solve(C, bt, rhs, dx, fixed_iter=1)
-    t_one = time.perf_counter() - t1
-    t2 = time.perf_counter()
-    O.solve(C, bt, rhs, dx, fixed_iter=2)
-    t_two = time.perf_counter() - t2
-    per_cycle = max(t_two - t_one, 1e-9)
-    setup = max(t_one - per_cycle, 0.0) + t_rhs
+    sample_cycles = 6
+    _, rep, _ = O.solve(C, bt, rhs, dx, fixed_iter=sample_cycles)
+    per_cycle = (rep.seconds - rep.setup_seconds) / sample_cycles
+    setup = rep.setup_seconds + t_rhs
     est = setup + per_cycle * cycles
     return {"value": est, "unit": "s", "cores": threads, "kind": "port",
             "sample": "oracle (C++ restatement of the reference CPU path, OpenMP) on %d host threads: RHS build + "
-                      "set-up + 1 and 2 fixed FP64 V-cycles at the full %d^3 size; solve time = set-up + "
-                      "per-cycle time x %d cycles (the FP64 cycle count of this input to 1e-8)" % (threads, n, cycles),
-            "per_cycle_s": per_cycle, "setup_s": setup, "sample_wall_s": t_rhs + t_one + t_two}
+                      "set-up + %d fixed FP64 V-cycles at the full %d^3 size; solve time = set-up + "
+                      "per-cycle time x %d cycles (the FP64 cycle count of this input to 1e-8)"
+                      % (threads, sample_cycles, n, cycles),
+            "per_cycle_s": per_cycle, "setup_s": setup, "sample_wall_s": time.perf_counter() - t0}
 
 
 def run_reference(args):

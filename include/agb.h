@@ -88,7 +88,8 @@ typedef struct agb_solver_opts {
     int krylov_dim;           /* FGMRES: basis size per cycle, <= 39 (20) */
     double inner_tol;         /* mixed FGMRES: residual reduction of one FP32 inner solve (1e-4) */
     int bottom_solver;        /* agb_bottom_solver (AGB_BOTTOM_BICGSTAB) */
-    int fine_kernel;          /* FP32 fine-level stencil kernels: 0 z-marching (default), 1 one thread per node */
+    int fine_kernel;          /* FP32 fine-level stencil kernels: 0 z-marching with TMA-staged stiffness
+                                 (default), 1 one thread per node, 2 z-marching with register-staged stiffness */
     int krylov_reorth;        /* FGMRES Gram-Schmidt: 1 re-orthogonalise once, 0 single pass (default) */
     int reserved_opts;
 } agb_solver_opts;

@@ -50,6 +50,7 @@ class Report(ctypes.Structure):
         ("rhsnorm0", ctypes.c_double),
         ("final_resnorm", ctypes.c_double),
         ("seconds", ctypes.c_double),
+        ("setup_seconds", ctypes.c_double),
     ]
 
 

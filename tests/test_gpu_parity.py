@@ -197,17 +197,37 @@ def test_vcycle_parity(agb, oracle, case, bottom):
 @pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm", "iso-randbc", "mm-randbc"])
 def test_zmarch_matches_per_node_kernels(agb, oracle, case):
     """The FP32 fine-level z-marching kernels (Fapply, Jacobi sweep,
-    residual) against the one-thread-per-node kernels: one FP32 V-cycle and
-    one FP32 Fapply give the same numbers to FP32 rounding."""
+    residual; TMA-staged and register-staged stiffness) against the
+    one-thread-per-node kernels: one FP32 V-cycle and one FP32 Fapply give
+    the same numbers to FP32 rounding."""
     C, F0, bc, dx = CASES[case]()
     n = C.shape[0]
     r = P.random_field((3, n, n, n), 91)
-    outs = []
-    for fk in (0, 1):
+    outs = {}
+    for fk in (0, 1, 2):
         with make_op(agb, C, bc, dx, fine_kernel=fk) as op:
-            outs.append((op.vcycle(r, precision="mixed"), op.Fapply_f32(r.astype(np.float32))))
-    assert rel(outs[0][1], outs[1][1]) <= 1e-6
-    assert rel(outs[0][0], outs[1][0]) <= 1e-5
+            outs[fk] = (op.vcycle(r, precision="mixed"), op.Fapply_f32(r.astype(np.float32)))
+    for fk in (0, 2):
+        assert rel(outs[fk][1], outs[1][1]) <= 1e-6
+        assert rel(outs[fk][0], outs[1][0]) <= 1e-5
+
+
+@pytest.mark.parametrize("dims", [(41, 19, 37), (3, 3, 3), (35, 9, 4), (66, 11, 97)])
+def test_zmarch_tma_ragged_grids(agb, oracle, dims):
+    """TMA-staged FP32 Fapply on grids whose interior does not fill the
+    32 x 8 tiles or the z chunks (partial tiles, a 1-node interior, a pitch
+    that needs padding) against the oracle's FP64 operator, to FP32
+    rounding; random boundary types exercise the separate face kernel."""
+    nx, ny, nz = dims
+    C = np.ascontiguousarray(agb.synth.voronoi_cubic(max(dims), 16, seed=5)[0][:nz, :ny, :nx])
+    bc = P.random_bc(77)
+    dx = np.array([1 / (nx - 1), 1 / (ny - 1), 1 / (nz - 1)])
+    u = P.random_field((3, nz, ny, nx), 78)
+    bt, _ = bc.tables()
+    ref = oracle.fapply(C, bt, u, dx)
+    with make_op(agb, C, bc, dx, fine_kernel=0) as op:
+        f = op.Fapply_f32(u.astype(np.float32))
+    assert rel(f, ref) <= 2e-6
 
 
 @pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
