@@ -18,7 +18,8 @@ EXPORTS = [
     "agb_elastic_restrict", "agb_elastic_prolong_add", "agb_elastic_vcycle", "agb_elastic_bc_init", "agb_elastic_build_rhs",
     "agb_linear_solve", "agb_newton_solve", "agb_elastic_stress_strain", "agb_profile_enable",
     "agb_profile_reset", "agb_profile_get", "agb_launch_count", "agb_cubic_stiffness", "agb_synth_uniform",
-    "agb_synth_inclusion_iso", "agb_synth_voronoi_cubic", "agb_synth_spheres_iso", "agb_status_string",
+    "agb_synth_inclusion_iso", "agb_synth_voronoi_cubic", "agb_synth_spheres_iso", "agb_synth_spheres_diffuse",
+    "agb_status_string",
     "agb_last_error", "agb_version", "agb_residual_norms_noalloc",
 ]
 

@@ -115,9 +115,12 @@ cudaError_t launch_from_double(const double* in, TO* out, int64_t n, double a, c
 namespace agb {
 // Dense direct bottom solve (nb = 3 N unknowns of the coarsest level):
 // work >= 4 nb^2 + 2 nb doubles, iwork >= 2 nb ints; flag[0] = 1 when a
-// pivot below `tiny` (the level's operator is singular to working precision).
-cudaError_t build_dense_inverse(int sym, const double* C, const LevelGeom<double>& G, const BcTable& bc,
-                                double* Ainv, double* work, int* iwork, int* flag, double tiny, cudaStream_t s);
+// pivot falls below 1e-12 max |diag| (written to tiny[0]): the level's
+// operator is singular to working precision.  Only kernels and a memset,
+// all argument values fixed, so the sequence can be captured in a graph.
+cudaError_t build_dense_inverse(int sym, const double* C, const double* diag, const LevelGeom<double>& G,
+                                const BcTable& bc, double* Ainv, double* work, int* iwork, int* flag, double* tiny,
+                                cudaStream_t s);
 cudaError_t launch_dense_bottom(const double* Ainv, const double* rhs, double* sol, int nb, cudaStream_t s);
 }  // namespace agb
 

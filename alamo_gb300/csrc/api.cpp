@@ -63,6 +63,11 @@ struct Lev {
     T* cor = nullptr;     // correction
     T* rescor = nullptr;  // res - A cor
     T* tmp = nullptr;     // Jacobi ping-pong buffer
+    // FP32 levels swept by the TMA stencil kernels: stiffness with the x
+    // pitch padded to 4 values and its tensor map
+    T* Cpad = nullptr;
+    CUtensorMap map{};
+    bool tma = false;
 };
 
 // Krylov space of the flexible GMRES: Arnoldi basis V (m+1 vectors), the
@@ -120,15 +125,16 @@ struct agb_elastic {
     double* dw = nullptr;  // 9N scratch of the Newton RHS
     Krylov<double> K64;
     Krylov<float> K32;
-    // FP32 fine-level stiffness with a padded x pitch and its TMA map
-    // (interior stencil kernels of fine_kernel 0)
-    float* c32pad = nullptr;
-    CUtensorMap cmap{};
-    bool have_cmap = false;
     // dense direct bottom solve
     double* bot_inv = nullptr;
     int bot_nb = 0;
     bool bot_dense = false;
+    // its build (assembly + Gauss-Jordan, 2 nb + 4 launches) as a graph,
+    // captured once per level layout and boundary table, and its buffers
+    cudaGraphExec_t bot_exec = nullptr;
+    cudaStream_t cap_stream = nullptr;
+    double* bot_work = nullptr;  // 4 nb^2 + 2 nb + 1 (threshold)
+    int* bot_iwork = nullptr;    // 2 nb + 1 (flag)
     // profiling
     bool prof = false;
     int64_t prof_count[AGB_K_NFAMILIES] = {0};
@@ -197,6 +203,7 @@ template <typename T>
 void free_levels(std::vector<Lev<T>>& L) {
     for (auto& l : L) {
         cudaFree(l.C); cudaFree(l.diag); cudaFree(l.res); cudaFree(l.cor); cudaFree(l.rescor); cudaFree(l.tmp);
+        cudaFree(l.Cpad);
     }
     L.clear();
 }
@@ -217,7 +224,10 @@ int num_levels(const int n0[3], int max_coarsening_level) {
     return lev;
 }
 
+void drop_bottom_graph(agb_elastic* h);
+
 agb_status alloc_levels64(agb_elastic* h) {
+    drop_bottom_graph(h);  // its kernels hold pointers into the levels
     free_levels(h->L64);
     const int nl = num_levels(h->n, h->opts.max_coarsening_level);
     h->ldx.assign(3 * nl, 0.0);
@@ -275,74 +285,98 @@ agb_status alloc_levels32(agb_elastic* h) {
 // Explicit inverse of the coarsest level's operator for the direct bottom
 // solve; falls back to BiCGStab (bot_dense = false) when it is too large or
 // singular to working precision.
+void drop_bottom_graph(agb_elastic* h) {
+    if (h->bot_exec) cudaGraphExecDestroy(h->bot_exec);
+    h->bot_exec = nullptr;
+}
+
 agb_status build_bottom_dense(agb_elastic* h) {
     Lev<double>& b = h->L64.back();
     const int nb = (int)(3 * b.G.N);
     if (nb > 4000) return AGB_OK;
     if (h->bot_nb != nb) {
+        drop_bottom_graph(h);
         cudaFree(h->bot_inv);
+        cudaFree(h->bot_work);
+        cudaFree(h->bot_iwork);
         h->bot_inv = nullptr;
+        h->bot_work = nullptr;
+        h->bot_iwork = nullptr;
+        h->bot_nb = 0;
         CK(cudaMalloc(&h->bot_inv, sizeof(double) * (size_t)nb * nb));
+        CK(cudaMalloc(&h->bot_work, sizeof(double) * (4 * (size_t)nb * nb + 2 * (size_t)nb + 1)));
+        CK(cudaMalloc(&h->bot_iwork, sizeof(int) * (2 * (size_t)nb + 1)));
         h->bot_nb = nb;
     }
-    double* work = nullptr;
-    int* iwork = nullptr;
-    CK(cudaMallocAsync((void**)&work, sizeof(double) * (4 * (size_t)nb * nb + 2 * (size_t)nb), h->stream));
-    CK(cudaMallocAsync((void**)&iwork, sizeof(int) * (2 * (size_t)nb + 1), h->stream));
-    // pivot threshold relative to the largest diagonal entry of the level
-    std::vector<double> dg(nb);
-    CK(cudaMemcpyAsync(dg.data(), b.diag, sizeof(double) * nb, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    double dmax = 0.0;
-    for (double v : dg) dmax = std::max(dmax, std::fabs(v));
-    int* flag = iwork + 2 * nb;
-    CK(build_dense_inverse(h->sym, b.C, b.G, h->bc, h->bot_inv, work, iwork, flag, 1e-12 * dmax, h->stream));
-    h->launches += 2 * nb + 3;
+    int* flag = h->bot_iwork + 2 * nb;
+    double* tiny = h->bot_work + 4 * (size_t)nb * nb + 2 * (size_t)nb;
+    if (!h->bot_exec) {
+        if (!h->cap_stream) CK(cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking));
+        CK(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
+        const cudaError_t e = build_dense_inverse(h->sym, b.C, b.diag, b.G, h->bc, h->bot_inv, h->bot_work,
+                                                  h->bot_iwork, flag, tiny, h->cap_stream);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(h->cap_stream, &g);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return fail(AGB_CUDA_ERROR, std::string("capture of the bottom-level inverse failed: ") +
+                                            cudaGetErrorString(e != cudaSuccess ? e : e2));
+        }
+        const cudaError_t e3 = cudaGraphInstantiate(&h->bot_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e3 != cudaSuccess) {
+            h->bot_exec = nullptr;
+            return fail(AGB_CUDA_ERROR, std::string("bottom-level graph: ") + cudaGetErrorString(e3));
+        }
+    }
+    CK(cudaGraphLaunch(h->bot_exec, h->stream));
+    h->launches += 2 * nb + 4;
     int hflag = 0;
     CK(cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaFreeAsync(work, h->stream));
-    CK(cudaFreeAsync(iwork, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->bot_dense = (hflag == 0);
     return AGB_OK;
 }
 
 // ---------------------------------------------------------------- prepare
-void free_pad(agb_elastic* h) {
-    cudaFree(h->c32pad);
-    h->c32pad = nullptr;
-    h->have_cmap = false;
-}
+// levels at least this large (nodes) are swept by the TMA stencil kernels;
+// on smaller ones the per-node kernels, one launch instead of two, are
+// faster
+static constexpr int64_t TMA_MIN_NODES = 30000;
 
-// FP32 copies of every level's stiffness and diagonal; for the TMA stencil
-// kernels also the padded fine-level copy and its tensor map
+// FP32 copies of every level's stiffness and diagonal; for the levels the
+// TMA stencil kernels sweep also the padded copy and its tensor map
 agb_status build_f32(agb_elastic* h) {
     const int nl = (int)h->L64.size();
     if (h->L32.size() != h->L64.size()) TRY(alloc_levels32(h));
     for (int l = 0; l < nl; l++) {
-        CK(launch_to_float(h->L64[l].C, h->L32[l].C, h->L64[l].G.N * h->nc, 1.0, h->stream));
-        CK(launch_diagonal<float>(h->sym, h->L32[l].C, h->L32[l].G, h->bc, h->L32[l].diag, h->stream));
+        Lev<float>& v = h->L32[l];
+        CK(launch_to_float(h->L64[l].C, v.C, h->L64[l].G.N * h->nc, 1.0, h->stream));
+        CK(launch_diagonal<float>(h->sym, v.C, v.G, h->bc, v.diag, h->stream));
         h->launches += 2;
-    }
-    const LevelGeom<float>& G = h->L32[0].G;
-    if (h->opts.fine_kernel == 0 && zmarch_tma_supported(G.nx, G.ny, G.nz)) {
-        if (!h->c32pad) {
+        const LevelGeom<float>& G = v.G;
+        const bool want = h->opts.fine_kernel == 0 && G.N >= TMA_MIN_NODES && zmarch_tma_supported(G.nx, G.ny, G.nz);
+        if (!want) {
+            cudaFree(v.Cpad);
+            v.Cpad = nullptr;
+            v.tma = false;
+            continue;
+        }
+        if (!v.Cpad) {
             const size_t bytes = sizeof(float) * h->nc * (size_t)G.nz * G.ny * zmarch_tma_pitch(G.nx);
-            if (cudaMalloc(&h->c32pad, bytes) != cudaSuccess) {
-                h->c32pad = nullptr;
+            if (cudaMalloc(&v.Cpad, bytes) != cudaSuccess) {
+                v.Cpad = nullptr;
                 cudaGetLastError();
                 return fail(AGB_OUT_OF_MEMORY, "allocation of the padded FP32 stiffness failed");
             }
-            h->have_cmap = false;
+            v.tma = false;
         }
-        CK(launch_pad_stiffness(h->L32[0].C, h->c32pad, G.nx, G.ny, G.nz, h->nc, h->stream));
+        CK(launch_pad_stiffness(v.C, v.Cpad, G.nx, G.ny, G.nz, h->nc, h->stream));
         h->launches++;
-        if (!h->have_cmap) {
-            CK(make_stiffness_map(h->c32pad, G.nx, G.ny, G.nz, h->nc, &h->cmap));
-            h->have_cmap = true;
+        if (!v.tma) {
+            CK(make_stiffness_map(v.Cpad, G.nx, G.ny, G.nz, h->nc, &v.map));
+            v.tma = true;
         }
-    } else if (h->c32pad) {
-        free_pad(h);
     }
     h->have_f32 = true;
     return AGB_OK;
@@ -384,33 +418,35 @@ struct Fam<double> { enum { J = AGB_K_JACOBI_F64, R = AGB_K_RESIDUAL_F64 }; };
 template <>
 struct Fam<float> { enum { J = AGB_K_JACOBI_F32, R = AGB_K_RESIDUAL_F32 }; };
 
-// the z-marching kernels serve the FP32 fine level (FP64 stays on the
-// per-node kernels: it is FP64-pipe bound and the z-march form spills):
-// fine_kernel 0 the TMA-staged kernels where the grid allows, else the
-// register-staged ones; 2 always the register-staged ones
+// the z-marching kernels serve FP32 levels (FP64 stays on the per-node
+// kernels: it is FP64-pipe bound and the z-march form spills):
+// fine_kernel 0: the TMA-staged kernels on every level large enough (see
+// build_f32); 2: the register-staged ones on the fine level; 1: none
 template <typename T>
-bool use_zm(const agb_elastic*, int) { return false; }
+bool use_zm(const agb_elastic*, const Lev<T>&, int) { return false; }
 template <>
-bool use_zm<float>(const agb_elastic* h, int l) { return l == 0 && h->opts.fine_kernel != 1; }
+bool use_zm<float>(const agb_elastic* h, const Lev<float>& v, int l) {
+    return h->opts.fine_kernel == 0 ? v.tma : (h->opts.fine_kernel == 2 && l == 0);
+}
 
-// FP32 fine-level stencil: mode 0 out = A x, 1 one Jacobi sweep, 2 residual
+// FP32 z-marching stencil on a level: mode 0 out = A x, 1 one Jacobi sweep,
+// 2 residual
 template <typename T>
-cudaError_t fine_zm(agb_elastic* h, int mode, const T* x, const T* C, const LevelGeom<T>& G, const T* b, const T* dg,
-                    T omega, T* out);
+cudaError_t level_zm(agb_elastic* h, const Lev<T>& v, int mode, const T* x, const T* b, const T* dg, T omega, T* out);
 template <>
-cudaError_t fine_zm<float>(agb_elastic* h, int mode, const float* x, const float* C, const LevelGeom<float>& G,
-                           const float* b, const float* dg, float omega, float* out) {
-    if (h->have_cmap && h->opts.fine_kernel == 0) {
+cudaError_t level_zm<float>(agb_elastic* h, const Lev<float>& v, int mode, const float* x, const float* b,
+                            const float* dg, float omega, float* out) {
+    if (v.tma && h->opts.fine_kernel == 0) {
         h->launches++;  // interior + faces
-        return launch_zmarch_tma(mode, h->sym, h->cmap, x, C, G, h->bc, b, dg, omega, out, h->bottom_info + 3,
+        return launch_zmarch_tma(mode, h->sym, v.map, x, v.C, v.G, h->bc, b, dg, omega, out, h->bottom_info + 3,
                                  h->stream);
     }
-    return launch_zmarch<float>(mode, h->sym, x, C, G, h->bc, b, dg, omega, out, h->stream);
+    return launch_zmarch<float>(mode, h->sym, x, v.C, v.G, h->bc, b, dg, omega, out, h->stream);
 }
 template <>
-cudaError_t fine_zm<double>(agb_elastic* h, int mode, const double* x, const double* C, const LevelGeom<double>& G,
-                            const double* b, const double* dg, double omega, double* out) {
-    return launch_zmarch<double>(mode, h->sym, x, C, G, h->bc, b, dg, omega, out, h->stream);
+cudaError_t level_zm<double>(agb_elastic* h, const Lev<double>& v, int mode, const double* x, const double* b,
+                             const double* dg, double omega, double* out) {
+    return launch_zmarch<double>(mode, h->sym, x, v.C, v.G, h->bc, b, dg, omega, out, h->stream);
 }
 
 // ncalls Fsmooth calls (2 sweeps each) on level l; cor_zero: cor is known 0
@@ -426,8 +462,8 @@ agb_status smooth(agb_elastic* h, std::vector<Lev<T>>& L, int l, int ncalls, boo
     for (int s = 0; s < sweeps; s++) {
         {
             ProfScope ps(h, Fam<T>::J, l == 0 && !(cor_zero && s == 0));
-            if (use_zm<T>(h, l) && !(cor_zero && s == 0))
-                CK(fine_zm<T>(h, 1, v.cor, v.C, v.G, v.res, v.diag, w, v.tmp));
+            if (use_zm<T>(h, v, l) && !(cor_zero && s == 0))
+                CK(level_zm<T>(h, v, 1, v.cor, v.res, v.diag, w, v.tmp));
             else
                 CK(launch_jacobi<T>(h->sym, (cor_zero && s == 0) ? nullptr : v.cor, v.res, v.diag, v.C, v.G, h->bc,
                                     w, v.tmp, h->stream));
@@ -487,8 +523,8 @@ agb_status vcycle(agb_elastic* h, std::vector<Lev<T>>& L) {
         TRY(smooth<T>(h, L, l, h->opts.pre_smooth, true));
         {
             ProfScope ps(h, Fam<T>::R, l == 0);
-            if (use_zm<T>(h, l))
-                CK(fine_zm<T>(h, 2, v.cor, v.C, v.G, v.res, nullptr, T(0), v.rescor));
+            if (use_zm<T>(h, v, l))
+                CK(level_zm<T>(h, v, 2, v.cor, v.res, nullptr, T(0), v.rescor));
             else
                 CK(launch_residual<T>(h->sym, v.cor, v.res, v.C, v.G, h->bc, v.rescor, nullptr, nullptr, h->stream));
         }
@@ -623,8 +659,8 @@ agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, doub
             if (out != K.Z[j]) CK(cudaMemcpyAsync(K.Z[j], out, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
         }
         // w = A Z_j
-        if (use_zm<T>(h, 0))
-            CK(fine_zm<T>(h, 0, K.Z[j], top.C, top.G, nullptr, nullptr, T(0), K.w));
+        if (use_zm<T>(h, top, 0))
+            CK(level_zm<T>(h, top, 0, K.Z[j], nullptr, nullptr, T(0), K.w));
         else
             CK(launch_fapply<T>(h->sym, K.Z[j], top.C, top.G, h->bc, K.w, st));
         // classical Gram-Schmidt, re-orthogonalised once unless krylov_reorth = 0
@@ -913,7 +949,6 @@ agb_status agb_elastic_destroy(agb_elastic* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     free_levels(h->L64);
     free_levels(h->L32);
-    free_pad(h);
     cudaFree(h->partials);
     cudaFree(h->norms_dev);
     if (h->norms_host) cudaFreeHost(h->norms_host);
@@ -923,7 +958,11 @@ agb_status agb_elastic_destroy(agb_elastic* h) {
     cudaFree(h->dw);
     h->K64.release();
     h->K32.release();
+    drop_bottom_graph(h);
     cudaFree(h->bot_inv);
+    cudaFree(h->bot_work);
+    cudaFree(h->bot_iwork);
+    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     for (int s = 0; s < 4; s++) cudaFree(h->io[s]);
     for (auto e : h->ev_pool) cudaEventDestroy(e);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -946,7 +985,6 @@ agb_status agb_elastic_set_opts(agb_elastic* h, const agb_solver_opts* o) {
             CK(cudaStreamSynchronize(h->stream));
         }
         free_levels(h->L32);
-        free_pad(h);
         h->have_f32 = false;
         agb_status st = alloc_levels64(h);
         if (st == AGB_OK && keep)
@@ -1012,6 +1050,7 @@ agb_status agb_elastic_set_bc(agb_elastic* h, const int* type, const double* val
         if (type[q] < AGB_BC_DISPLACEMENT || type[q] > AGB_BC_NONE) return fail(AGB_BAD_ARG, "unknown BC type");
     }
     for (int q = 0; q < 78; q++) { h->bc.t[q] = (unsigned char)type[q]; h->bcval[q] = val[q]; }
+    drop_bottom_graph(h);  // the boundary table is a kernel argument in it
     h->bc_set = true;
     h->prepared = false;
     h->have_f32 = false;
@@ -1067,8 +1106,8 @@ agb_status agb_elastic_fapply_f32(agb_elastic* h, int level, const float* u, flo
     TRY(dev_out(h, 1, f, bytes, where, &df));
     {
         ProfScope ps(h, AGB_K_FAPPLY_F32, level == 0);
-        if (use_zm<float>(h, level))
-            CK(fine_zm<float>(h, 0, (const float*)du, v.C, v.G, nullptr, nullptr, 0.f, (float*)df));
+        if (use_zm<float>(h, v, level))
+            CK(level_zm<float>(h, v, 0, (const float*)du, nullptr, nullptr, 0.f, (float*)df));
         else
             CK(launch_fapply<float>(h->sym, (const float*)du, v.C, v.G, h->bc, (float*)df, h->stream));
     }

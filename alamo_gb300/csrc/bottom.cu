@@ -248,7 +248,8 @@ __global__ void k_gj_init(const double* __restrict__ Acol, double* __restrict__ 
 // pivot of column k among the rows not used yet; prow = pivot row / pivot
 __global__ void __launch_bounds__(1024) k_gj_pivot(double* __restrict__ W, int nb, int k, int* __restrict__ used,
                                                    int* __restrict__ perm, double* __restrict__ prow,
-                                                   int* __restrict__ flag, double tiny) {
+                                                   int* __restrict__ flag, const double* __restrict__ tiny_p) {
+    const double tiny = tiny_p[0];
     __shared__ double bv[32];
     __shared__ int bi[32];
     double best = -1.0;
@@ -313,8 +314,26 @@ __global__ void k_gj_extract(const double* __restrict__ W, const int* __restrict
     }
 }
 
-cudaError_t build_dense_inverse(int sym, const double* C, const LevelGeom<double>& G, const BcTable& bc,
-                                double* Ainv, double* work, int* iwork, int* flag, double tiny, cudaStream_t s) {
+// tiny[0] = rel * max |diag|: the pivot threshold
+__global__ void __launch_bounds__(1024) k_pivot_threshold(const double* __restrict__ diag, int nb, double rel,
+                                                          double* __restrict__ tiny) {
+    __shared__ double sh[32];
+    double m = 0.0;
+    for (int r = threadIdx.x; r < nb; r += blockDim.x) m = fmax(m, fabs(diag[r]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = fmax(t, sh[w]);
+        tiny[0] = rel * t;
+    }
+}
+
+cudaError_t build_dense_inverse(int sym, const double* C, const double* diag, const LevelGeom<double>& G,
+                                const BcTable& bc, double* Ainv, double* work, int* iwork, int* flag, double* tiny,
+                                cudaStream_t s) {
     const int nb = (int)(3 * G.N);
     double* E = work;                          // nb*nb
     double* Acol = work + (int64_t)nb * nb;    // nb*nb
@@ -326,6 +345,7 @@ cudaError_t build_dense_inverse(int sym, const double* C, const LevelGeom<double
     if (sym == SYM_ISO) k_assemble<SYM_ISO><<<grd, 256, 0, s>>>(C, G, bc, E, Acol, nb);
     else k_assemble<SYM_MM><<<grd, 256, 0, s>>>(C, G, bc, E, Acol, nb);
     k_gj_init<<<152 * 4, 256, 0, s>>>(Acol, W, nb, used);
+    k_pivot_threshold<<<1, 1024, 0, s>>>(diag, nb, 1e-12, tiny);
     cudaMemsetAsync(flag, 0, sizeof(int), s);
     const int eb = nb < 152 * 8 ? nb : 152 * 8;
     for (int k = 0; k < nb; k++) {

@@ -369,11 +369,26 @@ template cudaError_t launch_prolong_add<float>(const float*, const LevelGeom<flo
                                                cudaStream_t);
 
 // ---------------------------------------------------------------- helpers
-__global__ void k_aos_to_soa(const double* __restrict__ a, double* __restrict__ s, int64_t N, int nc) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < N * nc; q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t node = q / nc;
-        const int c = (int)(q - node * nc);
-        s[c * N + node] = a[q];
+// AoS (N, nc) -> SoA (nc, N) through shared memory: a tile of 128 nodes is
+// read as one contiguous run and written as nc contiguous runs, both
+// coalesced (nc <= 21; the stride-nc shared reads are conflict-free per
+// half-warp for odd nc)
+static constexpr int TR_NODES = 128;
+__global__ void __launch_bounds__(256) k_aos_to_soa(const double* __restrict__ a, double* __restrict__ s, int64_t N,
+                                                    int nc) {
+    __shared__ double t[TR_NODES * 21];
+    const int64_t ntiles = (N + TR_NODES - 1) / TR_NODES;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t n0 = tile * TR_NODES;
+        const int nn = (int)(N - n0 < TR_NODES ? N - n0 : TR_NODES);
+        const double* src = a + n0 * nc;
+        for (int q = threadIdx.x; q < nn * nc; q += blockDim.x) t[q] = src[q];
+        __syncthreads();
+        for (int q = threadIdx.x; q < nn * nc; q += blockDim.x) {
+            const int c = q / nn, node = q - c * nn;
+            s[c * N + n0 + node] = t[node * nc + c];
+        }
+        __syncthreads();
     }
 }
 __global__ void k_soa_to_aos(const double* __restrict__ s, double* __restrict__ a, int64_t N, int nc) {
@@ -384,7 +399,9 @@ __global__ void k_soa_to_aos(const double* __restrict__ s, double* __restrict__ 
     }
 }
 cudaError_t launch_aos_to_soa(const double* aos, double* soa, int64_t N, int nc, cudaStream_t s) {
-    k_aos_to_soa<<<flat_blocks(N * nc), 256, 0, s>>>(aos, soa, N, nc);
+    if (nc > 21) return cudaErrorInvalidValue;
+    const int64_t tiles = (N + TR_NODES - 1) / TR_NODES;
+    k_aos_to_soa<<<(int)(tiles < 152 * 8 ? tiles : 152 * 8), 256, 0, s>>>(aos, soa, N, nc);
     return cudaGetLastError();
 }
 cudaError_t launch_soa_to_aos(const double* soa, double* aos, int64_t N, int nc, cudaStream_t s) {
@@ -493,7 +510,7 @@ __global__ void __launch_bounds__(256) k_rhs(const double* __restrict__ u, const
             for (int q = 0; q < 3; q++) s[p][q] = dw[(p * 3 + q) * N + id];
         const int reg = boundary_region<double>(cx, cy, cz, n);
 #pragma unroll
-        for (int r = 0; r < 3; r++) ret[r] = bc_component<double>(bc, reg, r, u[r * N + id], g, s, n);
+        for (int r = 0; r < 3; r++) ret[r] = bc_component<double>(bc.t, reg, r, u[r * N + id], g, s, n);
     } else {
         // div dw with central differences (src/Numeric/Stencil.H:588-657)
         const int64_t off[3] = {1, G.sy, G.sz};

@@ -78,53 +78,74 @@ __device__ __forceinline__ void stress_of(CF c, const T g[3][3], T s[3][3]) {
     }
 }
 
-// Row r of the boundary condition for region `reg`
+// Row r of the boundary condition for region `reg`; bt: the 78-entry type
+// table (region * 3 + component)
 template <typename T>
-__device__ __forceinline__ T bc_component(const BcTable& bc, int reg, int r, T ur, const T g[3][3], const T s[3][3],
-                                          const T n[3]) {
-    const int t = bc.t[reg * 3 + r];
+__device__ __forceinline__ T bc_component(const unsigned char* bt, int reg, int r, T ur, const T g[3][3],
+                                          const T s[3][3], const T n[3]) {
+    const int t = bt[reg * 3 + r];
     if (t == BC_DISP) return ur;
     if (t == BC_TRAC) return s[r][0] * n[0] + s[r][1] * n[1] + s[r][2] * n[2];
     if (t == BC_NEUMANN) return g[r][0] * n[0] + g[r][1] * n[1] + g[r][2] * n[2];
     return T(0);
 }
 
-// One-sided (first-order) or central first derivative at a node along axis d
-// (src/Numeric/Stencil.H:41-60, :70-191): forward at the low face, backward
-// at the high face.
+// One-sided (first-order) or central first derivative at a node along one
+// axis (src/Numeric/Stencil.H:41-60, :70-191): forward at the low face,
+// backward at the high face.  fp, f0, fm: the values at +1, 0, -1.
 template <typename T>
-__device__ __forceinline__ T d1_at(const T* __restrict__ f, int64_t id, int64_t s, int pos, int n, T h, T inv) {
-    if (pos == 0) return (f[id + s] - f[id]) * inv;
-    if (pos == n - 1) return (f[id] - f[id - s]) * inv;
-    return (f[id + s] - f[id - s]) * h;
+__device__ __forceinline__ T d1_of(T fp, T f0, T fm, int pos, int n, T h, T inv) {
+    if (pos == 0) return (fp - f0) * inv;
+    if (pos == n - 1) return (f0 - fm) * inv;
+    return (fp - fm) * h;
 }
 
-// Gradient g[p][q] = du_p/dx_q with the boundary-aware stencil
+// Gradient g[p][q] = du_p/dx_q with the boundary-aware stencil, from global
+// memory
 template <typename T>
 __device__ __forceinline__ void grad_at(const T* __restrict__ u, const LevelGeom<T>& G, int i, int j, int k, int64_t id,
                                         T g[3][3]) {
+    const int64_t sy = G.sy, sz = G.sz;
 #pragma unroll
     for (int p = 0; p < 3; p++) {
-        const T* up = u + p * G.N;
-        g[p][0] = d1_at(up, id, (int64_t)1, i, G.nx, G.h[0], G.inv[0]);
-        g[p][1] = d1_at(up, id, G.sy, j, G.ny, G.h[1], G.inv[1]);
-        g[p][2] = d1_at(up, id, G.sz, k, G.nz, G.h[2], G.inv[2]);
+        const T* f = u + p * G.N + id;
+        const T f0 = f[0];
+        g[p][0] = d1_of(i < G.nx - 1 ? f[1] : f0, f0, i > 0 ? f[-1] : f0, i, G.nx, G.h[0], G.inv[0]);
+        g[p][1] = d1_of(j < G.ny - 1 ? f[sy] : f0, f0, j > 0 ? f[-sy] : f0, j, G.ny, G.h[1], G.inv[1]);
+        g[p][2] = d1_of(k < G.nz - 1 ? f[sz] : f0, f0, k > 0 ? f[-sz] : f0, k, G.nz, G.h[2], G.inv[2]);
     }
 }
 
-// Apply the operator at a boundary node (i, j, k)
-template <typename T, int SYM, typename CF>
-__device__ __forceinline__ void apply_boundary(const T* __restrict__ u, const LevelGeom<T>& G, const BcTable& bc, CF c,
-                                               int i, int j, int k, int64_t id, T f[3]) {
+// BC rows of a boundary node (i, j, k).  U(p, a, b, c): component p of the
+// displacement at offset (a, b, c) from the node; c(e): stiffness entry e of
+// the node.  Offsets that leave the grid are never requested.
+template <typename T, int SYM, typename UA, typename CF>
+__device__ __forceinline__ void boundary_rows(UA U, CF c, const LevelGeom<T>& G, const unsigned char* bt, int i,
+                                              int j, int k, T f[3]) {
     T g[3][3], s[3][3], n[3];
-    grad_at(u, G, i, j, k, id, g);
+#pragma unroll
+    for (int p = 0; p < 3; p++) {
+        const T u0 = U(p, 0, 0, 0);
+        g[p][0] = d1_of(i < G.nx - 1 ? U(p, 1, 0, 0) : u0, u0, i > 0 ? U(p, -1, 0, 0) : u0, i, G.nx, G.h[0], G.inv[0]);
+        g[p][1] = d1_of(j < G.ny - 1 ? U(p, 0, 1, 0) : u0, u0, j > 0 ? U(p, 0, -1, 0) : u0, j, G.ny, G.h[1], G.inv[1]);
+        g[p][2] = d1_of(k < G.nz - 1 ? U(p, 0, 0, 1) : u0, u0, k > 0 ? U(p, 0, 0, -1) : u0, k, G.nz, G.h[2], G.inv[2]);
+    }
     stress_of<T, SYM>(c, g, s);
     const int cx = (i == 0) ? -1 : (i == G.nx - 1) ? 1 : 0;
     const int cy = (j == 0) ? -1 : (j == G.ny - 1) ? 1 : 0;
     const int cz = (k == 0) ? -1 : (k == G.nz - 1) ? 1 : 0;
     const int reg = boundary_region<T>(cx, cy, cz, n);
 #pragma unroll
-    for (int r = 0; r < 3; r++) f[r] = bc_component<T>(bc, reg, r, u[r * G.N + id], g, s, n);
+    for (int r = 0; r < 3; r++) f[r] = bc_component<T>(bt, reg, r, U(r, 0, 0, 0), g, s, n);
+}
+
+// Apply the operator at a boundary node (i, j, k) reading global memory
+template <typename T, int SYM, typename CF>
+__device__ __forceinline__ void apply_boundary(const T* __restrict__ u, const LevelGeom<T>& G, const BcTable& bc, CF c,
+                                               int i, int j, int k, int64_t id, T f[3]) {
+    const int64_t N = G.N, sy = G.sy, sz = G.sz;
+    auto U = [&](int p, int a, int b, int cc) { return u[p * N + id + a + sy * b + sz * cc]; };
+    boundary_rows<T, SYM>(U, c, G, bc.t, i, j, k, f);
 }
 
 // Interior-node arithmetic with the displacement and the stiffness read
@@ -273,7 +294,7 @@ __device__ __forceinline__ void diag_node(const T* __restrict__ C, const LevelGe
                     g[a][d] = v;
                 }
             stress_of<T, SYM>(cf, g, s);
-            dg[p] = bc_component<T>(bc, reg, p, T(1), g, s, n);
+            dg[p] = bc_component<T>(bc.t, reg, p, T(1), g, s, n);
         }
     } else {
         // (C : dgradgradu/du_p)_p with d2/dx_l^2 -> -2/dx_l^2 for component p

@@ -205,4 +205,65 @@ agb_status agb_synth_spheres_iso(int nx, int ny, int nz, const double dx[3], int
     return AGB_OK;
 }
 
+agb_status agb_synth_spheres_diffuse(int nx, int ny, int nz, const double dx[3], int nspheres, uint64_t seed,
+                                     double rmin, double rmax, double eps, double lam_in, double mu_in, double lam_out,
+                                     double mu_out, double smin, double smax, double* C, double* F0s, int* placed) {
+    if (!dx || !C || nspheres < 0 || rmin < 0 || rmax < rmin || !(eps > 0) || nx < 1 || ny < 1 || nz < 1)
+        return AGB_BAD_ARG;
+    Rng r(seed);
+    const double L[3] = {(nx - 1) * dx[0], (ny - 1) * dx[1], (nz - 1) * dx[2]};
+    struct S { double x, y, z, rad, s; };
+    std::vector<S> sp;
+    const int max_tries = 1000 * (nspheres + 1);
+    for (int t = 0; t < max_tries && (int)sp.size() < nspheres; t++) {
+        S c;
+        c.x = r.uniform() * L[0];
+        c.y = r.uniform() * L[1];
+        c.z = r.uniform() * L[2];
+        c.rad = r.uniform(rmin, rmax);
+        c.s = r.uniform(smin, smax);
+        bool ok = true;
+        for (const S& o : sp) {
+            const double ddx = c.x - o.x, ddy = c.y - o.y, ddz = c.z - o.z;
+            if (ddx * ddx + ddy * ddy + ddz * ddz < (c.rad + o.rad) * (c.rad + o.rad)) { ok = false; break; }
+        }
+        if (ok) sp.push_back(c);
+    }
+    const int64_t N = (int64_t)nx * ny * nz;
+    // eta (volume fraction of inclusion) accumulated in C[2q], eigenstrain in F0s
+    std::vector<double> eta(N, 0.0), f0(N, 0.0);
+    for (const S& c : sp) {
+        // the erf profile is below 1e-9 beyond r + 3 eps
+        const double ext = c.rad + 3.0 * eps;
+        const int i0 = std::max(0, (int)std::floor((c.x - ext) / dx[0]));
+        const int i1 = std::min(nx - 1, (int)std::ceil((c.x + ext) / dx[0]));
+        const int j0 = std::max(0, (int)std::floor((c.y - ext) / dx[1]));
+        const int j1 = std::min(ny - 1, (int)std::ceil((c.y + ext) / dx[1]));
+        const int k0 = std::max(0, (int)std::floor((c.z - ext) / dx[2]));
+        const int k1 = std::min(nz - 1, (int)std::ceil((c.z + ext) / dx[2]));
+#pragma omp parallel for schedule(static)
+        for (int k = k0; k <= k1; k++)
+            for (int j = j0; j <= j1; j++)
+                for (int i = i0; i <= i1; i++) {
+                    const double ddx = i * dx[0] - c.x, ddy = j * dx[1] - c.y, ddz = k * dx[2] - c.z;
+                    const double d = std::sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+                    // diffuse sphere of the reference's ellipse initial condition
+                    // (A = I / r^2): 0.5 - 0.5 erf((x A x - 1) / eps / |A x|)
+                    const double e = d > 0 ? 0.5 - 0.5 * std::erf((d * d - c.rad * c.rad) / (eps * d)) : 1.0;
+                    const int64_t id = i + (int64_t)nx * (j + (int64_t)ny * k);
+                    eta[id] += e;
+                    f0[id] += e * c.s;
+                }
+    }
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < N; q++) {
+        const double e = std::min(1.0, std::max(0.0, eta[q]));
+        C[2 * q] = (1.0 - e) * lam_out + e * lam_in;
+        C[2 * q + 1] = (1.0 - e) * mu_out + e * mu_in;
+        if (F0s) F0s[q] = f0[q];
+    }
+    if (placed) *placed = (int)sp.size();
+    return AGB_OK;
+}
+
 }  // extern "C"

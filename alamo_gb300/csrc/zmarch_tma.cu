@@ -1,11 +1,9 @@
-// FP32 fine-level stencil kernels with the stiffness staged by TMA.
+// FP32 stencil kernels of the multigrid levels with the stiffness staged by
+// TMA.
 //
-// Interior nodes (1..n-2 on every axis) are computed by a z-marching 32 x 8
-// thread block; the six boundary faces by a separate per-node kernel, so the
-// marching tiles start at node 1 and the 255 interior columns of a 257-node
-// axis fill 8 tiles of 32 exactly.
-//
-// Per z-plane a block needs
+// A 32 x 8 thread block marches its tile of interior columns (nodes 1..n-2 in
+// x and y, so the 255 interior columns of a 257-node axis fill 8 tiles of 32
+// exactly) through a chunk of z-planes.  Per plane it needs
 //   * the displacement of planes k-1, k, k+1 with a one-node x/y halo
 //     (3 x 10 x 34 values): a 4-slot ring filled by 4-byte cp.async, plane
 //     k+2 issued at the top of step k;
@@ -17,9 +15,12 @@
 //     registers from the previous step.
 // Everything the stencil reads then comes from shared memory at offsets that
 // are compile-time constants, and each array is read from HBM about once per
-// sweep.  The TMA box starts at x = x0 - 1 = 32 * blockIdx.x, a multiple of
-// 4 floats (16 bytes); the stiffness copy it reads has its x pitch padded to
-// a multiple of 4 floats so every global stride is a multiple of 16 bytes.
+// sweep.  The six boundary faces (2.3% of the nodes at 257^3) run in a
+// second, thin kernel: inside the marching blocks their branchy rows held
+// every step of the edge tiles back at the block barrier.  The TMA box
+// starts at x = x0 - 1 = 32 * blockIdx.x, a multiple of 4 floats (16 bytes);
+// the stiffness copy it reads has its x pitch padded to a multiple of 4
+// floats so every global stride is a multiple of 16 bytes.
 //
 // Every wait on an mbarrier is bounded: after the limit the block records
 // the failure in *err, stops marching (uniformly, through a shared flag),
@@ -193,6 +194,21 @@ __global__ void __launch_bounds__(NT, 2)
     cp_async_wait_all();
     __syncthreads();
 
+    // right-hand side and diagonal of the own column, loaded one plane ahead
+    // so their latency hides behind a whole step
+    float bq[3] = {0.f, 0.f, 0.f}, dq[3] = {1.f, 1.f, 1.f};
+    auto load_bd = [&](int kk, float bb[3], float dd[3]) {
+        if (col && kk < k1) {
+            const int64_t idk = i + sy * j + sz * (int64_t)kk;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                if (MODE >= 1) bb[c] = b[c * N + idk];
+                if (MODE == 1) dd[c] = dg[c * N + idk];
+            }
+        }
+    };
+    load_bd(k0, bq, dq);
+
     for (int k = k0; k < k1 && !abort_flag; k++) {
         if (k + 2 <= k1) {
             if (tid == 0) {
@@ -203,21 +219,16 @@ __global__ void __launch_bounds__(NT, 2)
             issued = k + 2;
         }
         const int64_t id = i + sy * j + sz * (int64_t)k;
-        float bq[3] = {0.f, 0.f, 0.f}, dq[3] = {1.f, 1.f, 1.f};
-        if (col) {
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                if (MODE >= 1) bq[c] = b[c * N + id];
-                if (MODE == 1) dq[c] = dg[c * N + id];
-            }
-        }
+        float bn[3] = {0.f, 0.f, 0.f}, dn[3] = {1.f, 1.f, 1.f};
+        load_bd(k + 1, bn, dn);
         const bool okn = mbar_wait(bar_u32 + 8u * ((k + 1) % CS), parity(k + 1));
         const float* cc = cslot(k);
         if (col && okn) {
             const float* cn = cslot(k + 1);
-            const float* u0 = Us + (k % US) * UPL + (ty + 1) * UHX + (tx + 1);
-            const float* um = Us + ((k + US - 1) % US) * UPL + (ty + 1) * UHX + (tx + 1);
-            const float* up = Us + ((k + 1) % US) * UPL + (ty + 1) * UHX + (tx + 1);
+            const int o = (ty + 1) * UHX + (tx + 1);
+            const float* u0 = Us + (k % US) * UPL + o;
+            const float* um = Us + ((k + US - 1) % US) * UPL + o;
+            const float* up = Us + ((k + 1) % US) * UPL + o;
             auto U = [&](int p, int a, int bb, int c) -> float {
                 const float* s = c == 0 ? u0 : (c < 0 ? um : up);
                 return s[p * (UHY * UHX) + bb * UHX + a];
@@ -245,6 +256,11 @@ __global__ void __launch_bounds__(NT, 2)
         }
 #pragma unroll
         for (int e = 0; e < NC; e++) Cp[e] = cc[e * CEL];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            bq[c] = bn[c];
+            dq[c] = dn[c];
+        }
         if (!okn) {
             abort_flag = 1;
             if (err) atomicExch(err, 1);
@@ -261,56 +277,53 @@ __global__ void __launch_bounds__(NT, 2)
     }
 }
 
-// Boundary faces: one thread per face node, the general BC rows.
-__device__ __forceinline__ void face_node(int64_t t, int nx, int ny, int nz, int& i, int& j, int& k) {
-    const int64_t fz = (int64_t)nx * ny, fy = (int64_t)nx * (nz - 2);
-    if (t < 2 * fz) {
-        k = t < fz ? 0 : nz - 1;
-        const int64_t r = t < fz ? t : t - fz;
-        j = (int)(r / nx);
-        i = (int)(r - (int64_t)j * nx);
-        return;
-    }
-    t -= 2 * fz;
-    if (t < 2 * fy) {
-        j = t < fy ? 0 : ny - 1;
-        const int64_t r = t < fy ? t : t - fy;
-        k = 1 + (int)(r / nx);
-        i = (int)(r % nx);
-        return;
-    }
-    t -= 2 * fy;
-    const int64_t fx = (int64_t)(ny - 2) * (nz - 2);
-    i = t < fx ? 0 : nx - 1;
-    const int64_t r = t < fx ? t : t - fx;
-    k = 1 + (int)(r / (ny - 2));
-    j = 1 + (int)(r % (ny - 2));
-}
-
+// Boundary faces: blockIdx.z picks the face (z = 0, z = nz-1, y = 0,
+// y = ny-1, x = 0, x = nx-1) and a 32 x 8 thread tile covers its two free
+// coordinates, the contiguous one across the warp where the face has one
+// (the x faces are strided in memory whatever the mapping).  Edges and
+// corners belong to the z faces, then to the y faces.  32-bit index
+// arithmetic; the boundary-type table is copied to shared memory with
+// constant offsets so no thread keeps a local copy of the parameter.
 template <int SYM, int MODE>
-__global__ void __launch_bounds__(256) k_zm_faces(const float* __restrict__ x, const float* __restrict__ C,
+__global__ void __launch_bounds__(256) k_zt_faces(const float* __restrict__ x, const float* __restrict__ C,
                                                   LevelGeom<float> G, BcTable bc, const float* __restrict__ b,
-                                                  const float* __restrict__ dg, float omega, float* __restrict__ out,
-                                                  int64_t nfaces) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nfaces;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        int i, j, k;
-        face_node(t, G.nx, G.ny, G.nz, i, j, k);
-        const int64_t id = i + G.sy * j + G.sz * (int64_t)k, N = G.N;
-        auto cf = [&](int a) { return C[a * N + id]; };
-        float r[3];
-        apply_boundary<float, SYM>(x, G, bc, cf, i, j, k, id, r);
+                                                  const float* __restrict__ dg, float omega,
+                                                  float* __restrict__ out) {
+    __shared__ unsigned char sbt[80];
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const int64_t q = c * N + id;
-            if (MODE == 0) {
-                out[q] = r[c];
-            } else if (MODE == 1) {
-                const float xv = x[q], d = dg[q];
-                out[q] = (1.f - omega) * xv + omega * (b[q] - (r[c] - xv * d)) / d;
-            } else {
-                out[q] = b[q] - r[c];
-            }
+        for (int q = 0; q < 78; q++) sbt[q] = bc.t[q];
+    }
+    __syncthreads();
+    const int f = blockIdx.z;
+    const int a = blockIdx.x * TX + threadIdx.x, c2 = blockIdx.y * TY + threadIdx.y;
+    int i, j, k;
+    if (f < 2) {
+        i = a; j = c2; k = f == 0 ? 0 : G.nz - 1;
+        if (i >= G.nx || j >= G.ny) return;
+    } else if (f < 4) {
+        i = a; k = 1 + c2; j = f == 2 ? 0 : G.ny - 1;
+        if (i >= G.nx || k > G.nz - 2) return;
+    } else {
+        j = 1 + a; k = 1 + c2; i = f == 4 ? 0 : G.nx - 1;
+        if (j > G.ny - 2 || k > G.nz - 2) return;
+    }
+    const int64_t N = G.N, sy = G.sy, sz = G.sz;
+    const int64_t id = i + sy * j + sz * (int64_t)k;
+    auto U = [&](int p, int da, int db, int dc) { return x[p * N + id + da + sy * db + sz * dc]; };
+    auto cf = [&](int e) { return C[e * N + id]; };
+    float r[3];
+    boundary_rows<float, SYM>(U, cf, G, sbt, i, j, k, r);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const int64_t q = c * N + id;
+        if (MODE == 0) {
+            out[q] = r[c];
+        } else if (MODE == 1) {
+            const float xv = x[q], d = dg[q];
+            out[q] = (1.f - omega) * xv + omega * (b[q] - (r[c] - xv * d)) / d;
+        } else {
+            out[q] = b[q] - r[c];
         }
     }
 }
@@ -325,7 +338,15 @@ __global__ void k_pad_planes(const float* __restrict__ src, float* __restrict__ 
     }
 }
 
-int zt_kchunk(int nz) { return nz >= 96 ? 32 : 16; }
+// planes per block: enough blocks for about two waves of two blocks per SM,
+// at least 4 planes (each block stages 3 extra planes), at most 32
+int zt_kchunk(int ni, int nj, int nk) {
+    const int64_t tiles = (int64_t)((ni + TX - 1) / TX) * ((nj + TY - 1) / TY);
+    int64_t kc = tiles * nk / (4 * 152);
+    if (kc < 4) kc = 4;
+    if (kc > 32) kc = 32;
+    return (int)kc;
+}
 
 }  // namespace
 
@@ -385,16 +406,15 @@ static cudaError_t zt_launch(const CUtensorMap& map, const float* x, const float
         if (e != cudaSuccess) return e;
         if (dev >= 0 && dev < 64) configured[dev] = true;
     }
-    const int kc = zt_kchunk(G.nz);
     const int ni = G.nx - 2, nj = G.ny - 2, nk = G.nz - 2;
+    const int kc = zt_kchunk(ni, nj, nk);
     dim3 blk(TX, TY, 1), grd((ni + TX - 1) / TX, (nj + TY - 1) / TY, (nk + kc - 1) / kc);
     k_zmarch_tma<SYM, MODE><<<grd, blk, bytes, s>>>(map, x, G, b, dg, omega, out, kc, err);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    const int64_t nf = G.N - (int64_t)ni * nj * nk;
-    int64_t fb = (nf + 255) / 256;
-    if (fb > 152 * 8) fb = 152 * 8;
-    k_zm_faces<SYM, MODE><<<(int)fb, 256, 0, s>>>(x, C, G, bc, b, dg, omega, out, nf);
+    const int fa = G.nx > G.ny ? G.nx : G.ny, fb = G.ny > G.nz ? G.ny : G.nz;
+    dim3 fgrd((fa + TX - 1) / TX, (fb + TY - 1) / TY, 6);
+    k_zt_faces<SYM, MODE><<<fgrd, blk, 0, s>>>(x, C, G, bc, b, dg, omega, out);
     return cudaGetLastError();
 }
 

@@ -72,3 +72,21 @@ def spheres_iso(n, nspheres=200, seed=1, rmin=0.02, rmax=0.06, contrast=10.0, sm
                                           ctypes.c_double(smin), ctypes.c_double(smax), _p(C), _p(F0),
                                           ctypes.byref(placed)))
     return C, F0, dx, placed.value
+
+
+def spheres_diffuse(n, nspheres=200, seed=1, rmin=0.02, rmax=0.06, eps=None, contrast=10.0, smin=0.0, smax=0.02,
+                    L_box=1.0):
+    """The spheres of spheres_iso with a diffuse interface (the reference's
+    ellipse initial condition); eps defaults to 4 node spacings."""
+    dx = L_box / (n - 1)
+    if eps is None:
+        eps = 4.0 * dx
+    C = np.empty((n, n, n, 2))
+    F0 = np.empty((n, n, n))
+    placed = ctypes.c_int()
+    L.check(L.lib().agb_synth_spheres_diffuse(n, n, n, _p(_dx(dx)), int(nspheres), ctypes.c_uint64(seed),
+                                              ctypes.c_double(rmin), ctypes.c_double(rmax), ctypes.c_double(eps),
+                                              ctypes.c_double(contrast), ctypes.c_double(contrast),
+                                              ctypes.c_double(1.0), ctypes.c_double(1.0), ctypes.c_double(smin),
+                                              ctypes.c_double(smax), _p(C), _p(F0), ctypes.byref(placed)))
+    return C, F0, dx, placed.value

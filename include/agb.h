@@ -271,6 +271,14 @@ agb_status agb_synth_voronoi_cubic(int nx, int ny, int nz, const double dx[3], i
 agb_status agb_synth_spheres_iso(int nx, int ny, int nz, const double dx[3], int nspheres, uint64_t seed, double rmin,
                                  double rmax, double lam_in, double mu_in, double lam_out, double mu_out, double smin,
                                  double smax, double* C, double* F0s, int* placed);
+/* The same spheres with the diffuse interface of the reference's ellipse
+ * initial condition (src/IC/Ellipse.H:56-75 with A = I / r^2): each sphere
+ * contributes eta = 0.5 - 0.5 erf((d^2 - r^2) / (eps d)) at distance d from
+ * its centre; the sum, clipped to [0, 1], mixes the two phases linearly
+ * (C = (1 - eta) C_out + eta C_in) and F0s = sum of eta_m s_m. */
+agb_status agb_synth_spheres_diffuse(int nx, int ny, int nz, const double dx[3], int nspheres, uint64_t seed,
+                                     double rmin, double rmax, double eps, double lam_in, double mu_in, double lam_out,
+                                     double mu_out, double smin, double smax, double* C, double* F0s, int* placed);
 
 const char* agb_status_string(int status);
 const char* agb_last_error(void);

@@ -406,9 +406,12 @@ def test_full_size_linearity_257(agb):
 @pytest.mark.slow
 def test_mixed_matches_fp64_129(agb):
     """Mixed-precision and FP64 solves of the 129^3 sphere medium agree to
-    the solve tolerance's scale."""
+    the solve tolerance's scale.  The spheres have the reference's diffuse
+    ellipse interface (4 node spacings): with a one-node jump of 10x the
+    reference's own V-cycle diverges on such media (see
+    test_reference_vcycle_diverges_on_sharp_spheres in the oracle tests)."""
     from alamo_gb300 import synth
-    C, F0, dx, _ = synth.spheres_iso(129, 30, seed=3, rmin=0.05, rmax=0.12)
+    C, F0, dx, _ = synth.spheres_diffuse(129, 30, seed=3, rmin=0.05, rmax=0.12)
     bc = __import__("alamo_gb300").bc.Constant()
     sols = []
     for prec in (0, 1):

@@ -102,3 +102,27 @@ def test_negative_real_eigenvalues_small_inclusion(oracle):
         d = oracle.diagonal(C, bt, dx).ravel()
         out[con] = np.linalg.eigvals(M / d[:, None]).real.min()
     assert out[10.0] < 0 < out[3.0]
+
+
+def test_reference_vcycle_diverges_on_sharp_spheres(oracle):
+    """Ten contrast-10 spheres with a one-node jump: the reference's V-cycle
+    iteration diverges from the first cycles.  The same spheres with the
+    reference's diffuse ellipse interface (2 node spacings) converge to
+    rounding.  Sphere media are therefore generated with the diffuse
+    interface (synth.spheres_diffuse)."""
+    from alamo_gb300 import synth
+    n = 33
+    bt, bv = __import__("alamo_gb300").bc.Constant().tables()
+    hists = {}
+    for eps in (0, 2):
+        if eps == 0:
+            C, F0, dx, placed = synth.spheres_iso(n, 10, seed=3, rmin=0.08, rmax=0.15)
+        else:
+            C, F0, dx, placed = synth.spheres_diffuse(n, 10, seed=3, rmin=0.08, rmax=0.15, eps=eps / (n - 1))
+        assert placed == 10
+        u = np.zeros((3, n, n, n))
+        rhs = oracle.build_rhs(C, F0, bt, u, oracle.bc_init(u, bt, bv), dx)
+        _, rep, hist = oracle.solve(C, bt, rhs, dx, fixed_iter=40)
+        hists[eps] = hist / hist[0]
+    assert hists[0][-1] > 1e3
+    assert hists[2][-1] < 1e-10
