@@ -393,7 +393,7 @@ cudaError_t launch_pad_stiffness(const float* C, float* Cpad, int nx, int ny, in
 template <int SYM, int MODE>
 static cudaError_t zt_launch(const CUtensorMap& map, const float* x, const float* C, const LevelGeom<float>& G,
                              const BcTable& bc, const float* b, const float* dg, float omega, float* out, int* err,
-                             cudaStream_t s) {
+                             cudaStream_t s, cudaStream_t s_faces) {
     constexpr int NC = SYM == SYM_ISO ? 2 : 21;
     constexpr int bytes = ZtSmem<NC>::total;
     static bool configured[64] = {};  // the attribute is set once per device
@@ -409,27 +409,28 @@ static cudaError_t zt_launch(const CUtensorMap& map, const float* x, const float
     const int ni = G.nx - 2, nj = G.ny - 2, nk = G.nz - 2;
     const int kc = zt_kchunk(ni, nj, nk);
     dim3 blk(TX, TY, 1), grd((ni + TX - 1) / TX, (nj + TY - 1) / TY, (nk + kc - 1) / kc);
-    k_zmarch_tma<SYM, MODE><<<grd, blk, bytes, s>>>(map, x, G, b, dg, omega, out, kc, err);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
     const int fa = G.nx > G.ny ? G.nx : G.ny, fb = G.ny > G.nz ? G.ny : G.nz;
     dim3 fgrd((fa + TX - 1) / TX, (fb + TY - 1) / TY, 6);
-    k_zt_faces<SYM, MODE><<<fgrd, blk, 0, s>>>(x, C, G, bc, b, dg, omega, out);
+    // faces first: on a separate stream they then overlap the interior sweep
+    k_zt_faces<SYM, MODE><<<fgrd, blk, 0, s_faces ? s_faces : s>>>(x, C, G, bc, b, dg, omega, out);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_zmarch_tma<SYM, MODE><<<grd, blk, bytes, s>>>(map, x, G, b, dg, omega, out, kc, err);
     return cudaGetLastError();
 }
 
 cudaError_t launch_zmarch_tma(int mode, int sym, const CUtensorMap& map, const float* x, const float* C,
                               const LevelGeom<float>& G, const BcTable& bc, const float* b, const float* dg,
-                              float omega, float* out, int* err, cudaStream_t s) {
+                              float omega, float* out, int* err, cudaStream_t s, cudaStream_t s_faces) {
     if (!zmarch_tma_supported(G.nx, G.ny, G.nz)) return cudaErrorInvalidValue;
     if (sym == SYM_ISO) {
-        if (mode == 0) return zt_launch<SYM_ISO, 0>(map, x, C, G, bc, b, dg, omega, out, err, s);
-        if (mode == 1) return zt_launch<SYM_ISO, 1>(map, x, C, G, bc, b, dg, omega, out, err, s);
-        return zt_launch<SYM_ISO, 2>(map, x, C, G, bc, b, dg, omega, out, err, s);
+        if (mode == 0) return zt_launch<SYM_ISO, 0>(map, x, C, G, bc, b, dg, omega, out, err, s, s_faces);
+        if (mode == 1) return zt_launch<SYM_ISO, 1>(map, x, C, G, bc, b, dg, omega, out, err, s, s_faces);
+        return zt_launch<SYM_ISO, 2>(map, x, C, G, bc, b, dg, omega, out, err, s, s_faces);
     }
-    if (mode == 0) return zt_launch<SYM_MM, 0>(map, x, C, G, bc, b, dg, omega, out, err, s);
-    if (mode == 1) return zt_launch<SYM_MM, 1>(map, x, C, G, bc, b, dg, omega, out, err, s);
-    return zt_launch<SYM_MM, 2>(map, x, C, G, bc, b, dg, omega, out, err, s);
+    if (mode == 0) return zt_launch<SYM_MM, 0>(map, x, C, G, bc, b, dg, omega, out, err, s, s_faces);
+    if (mode == 1) return zt_launch<SYM_MM, 1>(map, x, C, G, bc, b, dg, omega, out, err, s, s_faces);
+    return zt_launch<SYM_MM, 2>(map, x, C, G, bc, b, dg, omega, out, err, s, s_faces);
 }
 
 }  // namespace agb

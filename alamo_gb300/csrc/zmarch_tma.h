@@ -19,9 +19,12 @@ cudaError_t launch_pad_stiffness(const float* C, float* Cpad, int nx, int ny, in
 cudaError_t make_stiffness_map(const float* Cpad, int nx, int ny, int nz, int nc, CUtensorMap* map);
 // mode 0: out = A x; 1: one damped-Jacobi sweep (b, dg, omega); 2: out = b - A x.
 // C is the unpadded FP32 stiffness (boundary faces), map the padded copy's
-// tensor map (interior).  *err is set to 1 when a TMA wait gave up.
+// tensor map (interior).  *err is set to 1 when a TMA wait gave up.  The
+// interior kernel goes to s; the boundary-face kernel to s_faces when it is
+// not null (the caller orders s_faces after s's earlier work and s after
+// the faces), else to s before the interior.
 cudaError_t launch_zmarch_tma(int mode, int sym, const CUtensorMap& map, const float* x, const float* C,
                               const LevelGeom<float>& G, const BcTable& bc, const float* b, const float* dg,
-                              float omega, float* out, int* err, cudaStream_t s);
+                              float omega, float* out, int* err, cudaStream_t s, cudaStream_t s_faces);
 
 }  // namespace agb

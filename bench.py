@@ -50,8 +50,10 @@ BYTES_PER_NODE = {
 FAMILY = {"fapply_f64": 0, "jacobi_f64": 1, "residual_f64": 2, "fapply_f32": 3, "jacobi_f32": 4, "residual_f32": 5,
           "restrict": 6, "prolong": 7, "bottom": 8}
 # dram__bytes_read.sum + dram__bytes_write.sum per node of the fine-level
-# kernels, from the ncu captures summarised in profiles/ (None: not captured)
-TRAFFIC_PER_NODE = {}
+# interior sweep, from the 129^3 capture summarised in
+# profiles/k_zmarch_tma_jacobi_mm_129.md (283.9 MB + 19.3 MB over 2,146,689
+# nodes); the sweep streams every array once, so it scales with the nodes
+TRAFFIC_PER_NODE = {("jacobi_f32", 21): (283.893248e6 + 19.328e6) / 2146689}
 
 
 def parse():
