@@ -49,6 +49,10 @@ cudaError_t launch_prolong_add(const T* crse, const LevelGeom<T>& Gc, T* fine, c
 
 // layout and precision helpers
 cudaError_t launch_aos_to_soa(const double* aos, double* soa, int64_t N, int nc, cudaStream_t s);
+// (lambda, mu, F0) per node, SoA 3 x N: the isotropic entries or the Voigt
+// average of a major-minor tensor; F0 scalar (f0n 1) or trace / 3 (f0n 9)
+cudaError_t launch_guess_features(int sym, const double* C, int64_t N, const double* F0, int f0n, double* out,
+                                  cudaStream_t s);
 cudaError_t launch_soa_to_aos(const double* soa, double* aos, int64_t N, int nc, cudaStream_t s);
 cudaError_t launch_to_float(const double* in, float* out, int64_t n, double scale, cudaStream_t s);
 // out(double) += scale * in(float)

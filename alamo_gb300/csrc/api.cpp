@@ -27,6 +27,7 @@
 
 #include "agb_launch.h"
 #include "zmarch_tma.h"
+#include "unet_net.h"
 
 using namespace agb;
 
@@ -1329,6 +1330,59 @@ agb_status agb_newton_solve(agb_elastic* h, double* u, const double* b, const do
     if (s2 != AGB_OK) return s2;
     if (rep) rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return st;
+}
+
+agb_status agb_elastic_learned_guess(agb_elastic* h, agb_unet* net, const double* b, const double* F0, int f0_ncomp,
+                                     double* u, double norms[2], int* used, int where) {
+    if (!h || !net || !b || !u) return fail(AGB_BAD_ARG, "null argument");
+    if (!(f0_ncomp == 0 || f0_ncomp == 1 || f0_ncomp == 9) || (f0_ncomp && !F0))
+        return fail(AGB_BAD_ARG, "f0_ncomp must be 0, 1 or 9 (with F0 given)");
+    if (!h->model_set) return fail(AGB_NOT_READY, "model not set");
+    const int ng = unet_grid(net);
+    int lg = -1;
+    for (int l = 0; l < (int)h->L64.size(); l++) {
+        const LevelGeom<double>& G = h->L64[l].G;
+        if (G.nx == ng && G.ny == ng && G.nz == ng) { lg = l; break; }
+    }
+    if (lg < 0) return fail(AGB_BAD_ARG, "no multigrid level of the handle has the network's grid");
+    const int64_t N = nodes(h);
+    const size_t bytes = sizeof(double) * 3 * N;
+    const void *db = nullptr, *dF = nullptr;
+    TRY(dev_in(h, 1, b, bytes, where, &db));
+    if (f0_ncomp) TRY(dev_in(h, 3, F0, sizeof(double) * f0_ncomp * N, where, &dF));
+    // features on the fine level, restricted to the network's level (the
+    // levels' rescor buffers are free outside a solve); prediction in cor
+    std::vector<Lev<double>>& L = h->L64;
+    CK(launch_guess_features(h->sym, L[0].C, N, (const double*)dF, f0_ncomp, L[0].rescor, h->stream));
+    for (int l = 0; l < lg; l++) CK(launch_restrict<double>(L[l].rescor, L[l].G, L[l + 1].rescor, L[l + 1].G, h->stream));
+    h->launches += 1 + lg;
+    TRY(unet_predict_dev(net, L[lg].rescor, L[lg].cor, h->stream));
+    for (int l = lg - 1; l >= 0; l--) {
+        CK(cudaMemsetAsync(L[l].cor, 0, sizeof(double) * 3 * L[l].G.N, h->stream));
+        CK(launch_prolong_add<double>(L[l + 1].cor, L[l + 1].G, L[l].cor, L[l].G, h->stream));
+        h->launches++;
+    }
+    // fallback test on the Newton right-hand side at the guess and at zero
+    TRY(ensure_io(h, 2, 2 * bytes));
+    double* rhs = h->io[2];
+    double* zero = h->io[2] + 3 * N;
+    double ng_[2], nz_[2];
+    TRY(build_rhs_dev(h, L[0].cor, (const double*)db, (const double*)dF, f0_ncomp, rhs));
+    TRY(vec_norms(h, rhs, 3 * N, ng_));
+    CK(cudaMemsetAsync(zero, 0, bytes, h->stream));
+    TRY(build_rhs_dev(h, zero, (const double*)db, (const double*)dF, f0_ncomp, rhs));
+    TRY(vec_norms(h, rhs, 3 * N, nz_));
+    const bool ok = std::isfinite(ng_[0]) && ng_[0] <= nz_[0];
+    if (norms) { norms[0] = ng_[0]; norms[1] = nz_[0]; }
+    if (used) *used = ok ? 1 : 0;
+    const double* src = ok ? L[0].cor : zero;
+    if (where == AGB_MEM_DEVICE) {
+        CK(cudaMemcpyAsync(u, src, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    } else {
+        CK(cudaMemcpyAsync(u, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    return AGB_OK;
 }
 
 agb_status agb_elastic_stress_strain(agb_elastic* h, const double* u, const double* F0, int f0_ncomp, double* stress,

@@ -398,6 +398,40 @@ __global__ void k_soa_to_aos(const double* __restrict__ s, double* __restrict__ 
         a[q] = s[c * N + node];
     }
 }
+// (lambda, mu, F0) per node for the learned initial guess: the isotropic
+// entries, or the Voigt average of a major-minor tensor (K = (C11 + C22 + C33
+// + 2 (C12 + C13 + C23)) / 9, mu = (C11 + C22 + C33 - C12 - C13 - C23 + 3 (C44
+// + C55 + C66)) / 15, lambda = K - 2 mu / 3); F0 scalar or trace / 3
+__global__ void k_guess_features(int sym, const double* __restrict__ C, int64_t N, const double* __restrict__ F0,
+                                 int f0n, double* __restrict__ out) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < N; q += (int64_t)gridDim.x * blockDim.x) {
+        double lam, mu;
+        if (sym == SYM_ISO) {
+            lam = C[q];
+            mu = C[N + q];
+        } else {
+            auto c = [&](int a, int b) { return C[mm_ut(a, b) * N + q]; };
+            const double d = c(0, 0) + c(3, 3) + c(5, 5);
+            const double o = c(0, 3) + c(0, 5) + c(3, 5);
+            const double sh = c(4, 4) + c(2, 2) + c(1, 1);
+            const double K = (d + 2.0 * o) / 9.0;
+            mu = (d - o + 3.0 * sh) / 15.0;
+            lam = K - 2.0 * mu / 3.0;
+        }
+        double f = 0.0;
+        if (f0n == 1) f = F0[q];
+        else if (f0n == 9) f = (F0[9 * q] + F0[9 * q + 4] + F0[9 * q + 8]) / 3.0;
+        out[q] = lam;
+        out[N + q] = mu;
+        out[2 * N + q] = f;
+    }
+}
+cudaError_t launch_guess_features(int sym, const double* C, int64_t N, const double* F0, int f0n, double* out,
+                                  cudaStream_t s) {
+    k_guess_features<<<flat_blocks(N), 256, 0, s>>>(sym, C, N, F0, f0n, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_aos_to_soa(const double* aos, double* soa, int64_t N, int nc, cudaStream_t s) {
     if (nc > 21) return cudaErrorInvalidValue;
     const int64_t tiles = (N + TR_NODES - 1) / TR_NODES;

@@ -224,6 +224,43 @@ agb_status agb_residual_norms_noalloc(int nx, int ny, int nz, const double dx[3]
                                       const int* bc_type, const double* x, const double* b, double* r,
                                       double norms[2], void* stream);
 
+/* ------------------------------------------------ learned initial guess */
+/* No counterpart in the reference: a 3D U-Net (4 levels, 16/32/64/128
+ * channels, 3x3x3 convolutions + ReLU, nodal full-weighting down- and
+ * trilinear up-sampling, concatenated skips, 1x1x1 head) on the node grid of
+ * one multigrid level, BF16 activations and weights with FP32 accumulation
+ * on the tensor cores, FP32 master weights and Adam.  Inputs per node:
+ * lambda, mu and the dilatational eigenstrain F0; output: the displacement.
+ * n: nodes per axis of the network grid, 8 k + 1 >= 17 (65 for the trained
+ * model).  features / target / u: 3 x n^3 doubles, component-major
+ * (features: lambda, mu, F0).  Host or device pointers per `where`. */
+typedef struct agb_unet agb_unet;
+agb_status agb_unet_create(agb_unet** net, int n, uint64_t seed);
+agb_status agb_unet_destroy(agb_unet* net);
+agb_status agb_unet_num_params(const agb_unet* net, int64_t* count);
+/* all parameters as one FP32 vector (host memory), for saving and loading */
+agb_status agb_unet_get_params(agb_unet* net, float* out);
+agb_status agb_unet_set_params(agb_unet* net, const float* in);
+/* one Adam step (learning rate lr) on the mean squared error of one sample;
+ * *loss = the loss before the step (in units of (1e-3)^2) */
+agb_status agb_unet_train_step(agb_unet* net, const double* features, const double* target, float lr, double* loss,
+                               int where);
+agb_status agb_unet_predict(agb_unet* net, const double* features, double* u, int where);
+/* Initial guess for agb_newton_solve on the handle's grid: the model's
+ * (lambda, mu) -- the Voigt average for a major-minor model -- and F0 (its
+ * trace / 3 for 9 components) are restricted to the multigrid level whose
+ * grid is the network's, the prediction is prolongated back to the fine
+ * level and written to u.  Fallback: when the Newton right-hand side at the
+ * guess, b - A(u), has a larger inf-norm than at u = 0, u is set to zero and
+ * *used = 0.  norms[0] = that norm at the guess, norms[1] = at zero. */
+agb_status agb_elastic_learned_guess(agb_elastic* h, agb_unet* net, const double* b, const double* F0, int f0_ncomp,
+                                     double* u, double norms[2], int* used, int where);
+/* Test hook of the tensor-core convolution: X [V][Cin] BF16 channels-last
+ * (device), W [Cout][Cin][27] FP32, bias [Cout] FP32 (may be NULL), output
+ * Y (BF16) or Yf (FP32), exactly one non-NULL; stream may be NULL. */
+agb_status agb_conv3_bf16(const void* X, int Cin, const float* W, const float* bias, int Cout, int nx, int ny, int nz,
+                          int relu, void* Y, float* Yf, void* stream);
+
 /* --------------------------------------------------------- profiling */
 /* Kernel families timed with CUDA events on the handle's stream when
  * profiling is on (fine level only). */
