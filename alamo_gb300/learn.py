@@ -17,7 +17,7 @@ import numpy as np
 from . import _lib as L
 from . import bc as B
 from . import synth
-from .elastic import DevicePtr, Elastic, Newton, _arg, _same_where, default_opts
+from .elastic import DevicePtr, Elastic, Linear, Newton, _arg, _same_where, default_opts
 
 
 class UNet:
@@ -83,13 +83,17 @@ class UNet:
         return u
 
 
-def learned_guess(op, net, b, F0=None, u=None):
-    """agb_elastic_learned_guess: (u, norms at guess / at zero, used)."""
+def learned_guess(op, net, b, F0=None, u=None, rhs=None):
+    """agb_elastic_learned_guess: (u, rhs, (norm at guess, at zero), used);
+    solve A u = rhs from u (agb_linear_solve) for the Newton step from 0."""
     n = op._vec_shape(0)
     if u is None:
         u = np.empty(n)
+    if rhs is None and not isinstance(u, DevicePtr):
+        rhs = np.empty(n)
     pb, wb = _arg(b)
     pu, wu = _arg(u)
+    pr, wr = _arg(rhs)
     f0n, pF, wF = 0, None, None
     if F0 is not None:
         if isinstance(F0, tuple):
@@ -99,9 +103,9 @@ def learned_guess(op, net, b, F0=None, u=None):
             f0n = 1 if F0.ndim == 3 else 9
     norms = (ctypes.c_double * 2)()
     used = ctypes.c_int()
-    L.check(L.lib().agb_elastic_learned_guess(op.h, net.h, pb, pF, f0n, pu, norms, ctypes.byref(used),
-                                              _same_where(wb, wu, wF)))
-    return u, (norms[0], norms[1]), bool(used.value)
+    L.check(L.lib().agb_elastic_learned_guess(op.h, net.h, pb, pF, f0n, pu, pr, norms, ctypes.byref(used),
+                                              _same_where(wb, wu, wF, wr if rhs is not None else None)))
+    return u, rhs, (norms[0], norms[1]), bool(used.value)
 
 
 def features_of(C, F0):
@@ -113,15 +117,20 @@ def features_of(C, F0):
     return f
 
 
+# diffuse-interface width of the inclusion media: 2 node spacings of the
+# 65^3 training grid, the same physical width at every resolution
+EPS_INCLUSION = 2.0 / 64.0
+
+
 def inclusion_medium(n, rng):
     """One random inclusion medium of the training distribution: count
     U{1..40}, radius U[0.03, 0.15], contrast log-U[1, 20] (lambda = mu =
     contrast inside, 1 outside), eigenstrain U[0, 0.02] per inclusion, with
-    the reference's diffuse interface over 2 node spacings."""
+    the reference's diffuse interface (EPS_INCLUSION)."""
     count = int(rng.integers(1, 41))
     contrast = float(np.exp(rng.uniform(0.0, np.log(20.0))))
     seed = int(rng.integers(1, 2 ** 62))
-    C, F0, dx, placed = synth.spheres_diffuse(n, count, seed=seed, rmin=0.03, rmax=0.15, eps=2.0 / (n - 1),
+    C, F0, dx, placed = synth.spheres_diffuse(n, count, seed=seed, rmin=0.03, rmax=0.15, eps=EPS_INCLUSION,
                                               contrast=contrast, smin=0.0, smax=0.02)
     return C, F0, dx
 
@@ -195,3 +204,93 @@ def train(net, feats, sols, epochs=3, lr=1e-3, lr_end=1e-4, seed=0, log=None):
         if log:
             log("epoch %d  mean loss %.4e" % (ep, hist[-1]))
     return hist
+
+
+def guess_and_solve(n, C, F0, bc, dx, net=None, tol=1e-8, sym="isotropic"):
+    """Mixed FGMRES Newton solve of one medium from the learned guess (net
+    given) or from zero; returns (u, report, seconds, guess info).  Times the
+    whole call on the host, guess included (GPU work is synchronous)."""
+    import time
+    nlev = _levels(n)
+    o = default_opts(precision="mixed", solver="fgmres", bottom_solver="direct", max_coarsening_level=max(nlev - 2, 0))
+    with Elastic(n, dx, sym, o) as op:
+        op.SetModel(np.ascontiguousarray(C))
+        op.SetBC(bc)
+        b = op.bc_init()
+        op.prepareForSolve()
+        t0 = time.perf_counter()
+        info = None
+        if net is not None:
+            u, rhs, norms, used = learned_guess(op, net, b, F0)
+            info = {"used": used, "restricted_residual_guess": norms[0], "restricted_residual_zero": norms[1],
+                    "guess_s": time.perf_counter() - t0}
+            rep = Linear(op).solve(u, rhs, tol, 0.0, allow_not_converged=True)
+        else:
+            u = np.zeros((3, n, n, n))
+            rep = Newton(op).solve(u, b, F0, tol_rel=tol, tol_abs=0.0, allow_not_converged=True)
+        sec = time.perf_counter() - t0
+    return u, rep, sec, info
+
+
+def _main():
+    import argparse
+    import json
+    import os
+    import time
+    ap = argparse.ArgumentParser(description="train / evaluate the learned initial guess")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    tr = sub.add_parser("train")
+    tr.add_argument("--samples", type=int, default=2000)
+    tr.add_argument("--epochs", type=int, default=3)
+    tr.add_argument("--lr", type=float, default=1e-3)
+    tr.add_argument("--seed", type=int, default=1)
+    tr.add_argument("--out", required=True)
+    ev = sub.add_parser("evaluate")
+    ev.add_argument("--weights", required=True)
+    ev.add_argument("--n", type=int, default=129)
+    ev.add_argument("--count", type=int, default=5)
+    ev.add_argument("--seed", type=int, default=1000003)
+    ev.add_argument("--voronoi", type=int, default=0, help="grains of an out-of-distribution polycrystal (config 5)")
+    a = ap.parse_args()
+    import torch
+    dev = torch.device("cuda", 0)
+    if a.cmd == "train":
+        t0 = time.time()
+        feats, sols = make_dataset(a.samples, 65, seed=a.seed, device=dev)
+        t1 = time.time()
+        with UNet(65, seed=a.seed) as net:
+            hist = train(net, feats, sols, epochs=a.epochs, lr=a.lr, log=print)
+            net.save(a.out)
+        print(json.dumps({"samples": a.samples, "epochs": a.epochs, "dataset_s": t1 - t0, "train_s": time.time() - t1,
+                          "loss_per_epoch": hist, "params": int(np.load(a.out).size)}))
+        return
+    net = UNet(65)
+    net.load(a.weights)
+    rng = np.random.default_rng(a.seed)
+    rows = []
+    for k in range(a.count):
+        if a.voronoi:
+            Cm, dx = synth.voronoi_cubic(a.n, a.voronoi, seed=int(rng.integers(1, 2 ** 31)))
+            F0, bc, sym = None, B.TensionTest("uniaxial_stress_clamp", disp=0.01), "majorminor"
+            C = Cm
+        else:
+            C, F0, dx = inclusion_medium(a.n, rng)
+            bc, sym = B.Constant(), "isotropic"
+        u0, r0, s0, _ = guess_and_solve(a.n, C, F0, bc, dx, None, sym=sym)
+        u1, r1, s1, info = guess_and_solve(a.n, C, F0, bc, dx, net, sym=sym)
+        err = float(np.abs(u1 - u0).max() / max(np.abs(u0).max(), 1e-300))
+        rows.append({"zero": {"cycles": r0["iters"], "s": s0, "status": r0["status"]},
+                     "guess": {"cycles": r1["iters"], "s": s1, "status": r1["status"], **info},
+                     "solution_rel_diff": err})
+        print(json.dumps(rows[-1]), flush=True)
+    used = [r["guess"]["used"] for r in rows]
+    print(json.dumps({"n": a.n, "count": a.count, "voronoi": a.voronoi, "fallback_rate": 1 - float(np.mean(used)),
+                      "cycles_zero": float(np.mean([r["zero"]["cycles"] for r in rows])),
+                      "cycles_guess": float(np.mean([r["guess"]["cycles"] for r in rows])),
+                      "s_zero": float(np.mean([r["zero"]["s"] for r in rows])),
+                      "s_guess": float(np.mean([r["guess"]["s"] for r in rows]))}))
+    net.close()
+
+
+if __name__ == "__main__":
+    _main()

@@ -7,15 +7,17 @@ is major-minor (21 values per node).  Synthetic inputs, seeded.
 
 One step = one complete solve from the inputs resident in HBM: SetModel
 (stiffness layout change), prepareForSolve (stiffness coarsening, diagonals,
-bottom-level inverse), the Newton right-hand side and the solve to 1e-8
-relative residual (inf-norm of the FP64 residual, tol_abs = 0).  Fast path:
-FGMRES preconditioned by one V-cycle, both in FP32, inside FP64 iterative
-refinement, with a direct solve on a 5^3-node bottom level.  The plain FP64
-comparison is the reference's algorithm on the GPU: V(2,2) cycles with
-damped Jacobi and the BiCGStab bottom, everything FP64.  `value` is seconds per solve (lower is better); `e2e` is the same
-solve through the C ABI with host buffers (stiffness and right-hand side
-copied in, displacement copied out, inside the timed region).  The plain FP64
-V-cycle solve of the same input is timed beside it (`plain_fp64_s`).
+bottom-level inverse), the learned initial guess (U-Net on the 65^3 level,
+with its residual-based fallback to zero; --guess '' skips it), the Newton
+right-hand side and the solve to 1e-8 relative residual (inf-norm of the
+FP64 residual, tol_abs = 0).  Fast path: FGMRES preconditioned by one
+V-cycle, both in FP32, inside FP64 iterative refinement, with a direct solve
+on a 5^3-node bottom level.  The plain FP64 comparison is the reference's
+algorithm on the GPU: V(2,2) cycles with damped Jacobi and the BiCGStab
+bottom, everything FP64, from zero.  `value` is seconds per solve (lower is
+better); `e2e` is the same solve through the C ABI with host buffers
+(stiffness and right-hand side copied in, displacement copied out, inside
+the timed region).
 
 --impl reference times the reference's CPU path restated in oracle/ (the
 reference itself needs AMReX and cannot be built) on all host cores.
@@ -72,6 +74,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--n", type=int, default=0, help="override the grid size (nodes per axis)")
+    p.add_argument("--guess", default=os.path.join(ROOT, "alamo_gb300", "weights", "unet65.npy"),
+                   help="U-Net weights of the learned initial guess ('' = solve from zero)")
     return p.parse_args()
 
 
@@ -262,16 +266,36 @@ def main():
     F0arg = (P(F0_dev.data_ptr()), 1) if F0_dev is not None else None
     newton = A.Newton(op)
     reports = []
+    guesses = []
+    net = None
+    if args.guess and os.path.exists(args.guess):
+        from alamo_gb300 import learn
+        net = learn.UNet(65)
+        net.load(args.guess)
+
+    rhs_dev = torch.zeros_like(u_dev) if net is not None else None
+    linear = A.Linear(op)
 
     def step():
         op.SetModel(P(C_dev.data_ptr()))
-        with torch.cuda.stream(stream):
-            u_dev.zero_()
-        reports.append(newton.solve(P(u_dev.data_ptr()), P(b_dev.data_ptr()), F0arg, tol_rel=1e-8, tol_abs=0.0))
+        if net is not None:
+            # learned initial guess with its residual-based fallback (zero
+            # when the fallback fires) as the first iterate of the Newton
+            # step's linear solve
+            _, _, norms, used = learn.learned_guess(op, net, P(b_dev.data_ptr()), F0arg, P(u_dev.data_ptr()),
+                                                    P(rhs_dev.data_ptr()))
+            guesses.append({"used": used, "rhs_guess": norms[0], "rhs_zero": norms[1]})
+            reports.append(linear.solve(P(u_dev.data_ptr()), P(rhs_dev.data_ptr()), 1e-8, 0.0))
+        else:
+            with torch.cuda.stream(stream):
+                u_dev.zero_()
+            reports.append(newton.solve(P(u_dev.data_ptr()), P(b_dev.data_ptr()), F0arg, tol_rel=1e-8,
+                                        tol_abs=0.0))
 
     for _ in range(args.warmup):
         step()
     reports.clear()
+    guesses.clear()
     op.profile(True)
     launches0 = op.launch_count()
     clocks = Clocks(local)
@@ -318,11 +342,17 @@ def main():
         u_h = torch.zeros_like(b_h).pin_memory()
         F0_h = torch.from_numpy(F0).pin_memory() if F0 is not None else None
 
+        rhs_h = torch.zeros_like(b_h).pin_memory()
+
         def step_host():
             op.SetModel(C_h.numpy())
-            u_h.zero_()
-            newton.solve(u_h.numpy(), b_h.numpy(), F0_h.numpy() if F0_h is not None else None, tol_rel=1e-8,
-                         tol_abs=0.0)
+            F0x = F0_h.numpy() if F0_h is not None else None
+            if net is not None:
+                learn.learned_guess(op, net, b_h.numpy(), F0x, u_h.numpy(), rhs_h.numpy())
+                linear.solve(u_h.numpy(), rhs_h.numpy(), 1e-8, 0.0)
+            else:
+                u_h.zero_()
+                newton.solve(u_h.numpy(), b_h.numpy(), F0x, tol_rel=1e-8, tol_abs=0.0)
 
         step_host()
         barrier()
@@ -336,9 +366,16 @@ def main():
         te = torch.tensor([wall], dtype=torch.float64, device=dev)
         if dist is not None:
             dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        h2d = C.nbytes + 2 * 3 * N * 8 + (F0.nbytes if F0 is not None else 0)
+        vec = 3 * N * 8
+        if net is not None:
+            # guess: b, F0 in; guess and right-hand side out; solve: both in, u out
+            h2d = C.nbytes + 3 * vec + (F0.nbytes if F0 is not None else 0)
+            d2h = 3 * vec
+        else:
+            h2d = C.nbytes + 2 * vec + (F0.nbytes if F0 is not None else 0)
+            d2h = vec
         e2e = {"value": float(te.item()), "unit": "s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(3 * N * 8), "timing": "host wall clock around synchronous C-ABI calls"}
+               "d2h_bytes_per_step": int(d2h), "timing": "host wall clock around synchronous C-ABI calls"}
 
     # plain FP64 V-cycle solve of the same input
     plain = None
@@ -389,7 +426,8 @@ def main():
 
     rep = reports[-1] if reports else {}
     line = {
-        "metric": "solve time to 1e-8 rel. residual @%d^3: mixed FP32/FP64 vs plain FP64; Fapply HBM GB/s" % n,
+        "metric": "solve time to 1e-8 rel. residual @%d^3: %smixed FP32/FP64 vs plain FP64; Fapply HBM GB/s"
+                  % (n, "learned guess + " if net is not None else ""),
         "value": sec, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-cycle/f64-refinement" if prec else "f64", "data": "synthetic",
@@ -398,6 +436,11 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single-gpu",
                    "l2": "inputs larger than L2 (%.1f GB of stiffness)" % (C.nbytes / 1e9)},
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": ck,
+        "guess": ({"weights": os.path.relpath(args.guess, ROOT), "network_grid": 65,
+                   "used_fraction": float(np.mean([g["used"] for g in guesses])) if guesses else None,
+                   "restricted_rhs_at_guess": guesses[-1]["rhs_guess"] if guesses else None,
+                   "restricted_rhs_at_zero": guesses[-1]["rhs_zero"] if guesses else None}
+                  if net is not None else None),
         "solve": {"v_cycles": rep.get("iters"), "fp64_residuals": rep.get("fp64_residuals"),
                   "final_rel_resnorm_l2": (rep.get("final_resnorm_l2", 0) / rep["rhsnorm_l2"]) if rep else None,
                   "final_rel_resnorm": (rep.get("final_resnorm", 0) / rep["rhsnorm0"]) if rep else None,

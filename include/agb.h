@@ -246,15 +246,20 @@ agb_status agb_unet_set_params(agb_unet* net, const float* in);
 agb_status agb_unet_train_step(agb_unet* net, const double* features, const double* target, float lr, double* loss,
                                int where);
 agb_status agb_unet_predict(agb_unet* net, const double* features, double* u, int where);
-/* Initial guess for agb_newton_solve on the handle's grid: the model's
- * (lambda, mu) -- the Voigt average for a major-minor model -- and F0 (its
- * trace / 3 for 9 components) are restricted to the multigrid level whose
- * grid is the network's, the prediction is prolongated back to the fine
- * level and written to u.  Fallback: when the Newton right-hand side at the
- * guess, b - A(u), has a larger inf-norm than at u = 0, u is set to zero and
- * *used = 0.  norms[0] = that norm at the guess, norms[1] = at zero. */
+/* Initial iterate for the linear solve of a Newton step from zero, on the
+ * handle's grid: the model's (lambda, mu) -- the Voigt average for a
+ * major-minor model -- and F0 (its trace / 3 for 9 components) are
+ * restricted to the multigrid level whose grid is the network's, the
+ * prediction is prolongated back to the fine level and written to u; rhs
+ * (may be NULL) receives the Newton right-hand side at zero, so
+ * agb_linear_solve(h, u, rhs, ...) then solves A u = rhs from the guess and
+ * converges to the same displacement as agb_newton_solve from zero.
+ * Fallback: when rhs - A u, restricted to the network's level (the smooth
+ * part the multigrid cycles reduce slowly), has a larger 2-norm than rhs
+ * itself, u is set to zero and *used = 0.  norms[0] = that norm at the
+ * guess, norms[1] = at zero. */
 agb_status agb_elastic_learned_guess(agb_elastic* h, agb_unet* net, const double* b, const double* F0, int f0_ncomp,
-                                     double* u, double norms[2], int* used, int where);
+                                     double* u, double* rhs, double norms[2], int* used, int where);
 /* Test hook of the tensor-core convolution: X [V][Cin] BF16 channels-last
  * (device), W [Cout][Cin][27] FP32, bias [Cout] FP32 (may be NULL), output
  * Y (BF16) or Yf (FP32), exactly one non-NULL; stream may be NULL. */

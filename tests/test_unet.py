@@ -185,8 +185,8 @@ def test_unet_train_step_follows_autograd(agb):
 def test_learned_guess_transfers_and_fallback(agb, oracle):
     """The guess is the prediction on the network's level (features restricted
     from the fine grid with the multigrid weights) prolongated back; when the
-    Newton right-hand side at the guess exceeds that at zero the guess is
-    dropped."""
+    Newton right-hand side at the guess, restricted to the network's level,
+    exceeds that at zero the guess is dropped."""
     from alamo_gb300 import learn
     n = 33
     C, F0, bc, dx = P.c1(n)
@@ -194,18 +194,26 @@ def test_learned_guess_transfers_and_fallback(agb, oracle):
         op.SetModel(np.ascontiguousarray(C))
         op.SetBC(bc)
         b = op.bc_init()
-        u, (rg, r0), used = learn.learned_guess(op, net, b, F0)
+        u, rhs, (rg, r0), used = learn.learned_guess(op, net, b, F0)
         f = learn.features_of(C, F0)
         pred = net.predict(oracle.restrict(f))
         expect = oracle.prolong_add(pred, np.zeros((3, n, n, n)))
         bt, _ = bc.tables()
-        rhs_g = oracle.build_rhs(C, F0, bt, expect, b, dx)
-        rhs_0 = oracle.build_rhs(C, F0, bt, np.zeros_like(expect), b, dx)
-        assert abs(rg - np.abs(rhs_g).max()) <= 1e-10 * np.abs(rhs_g).max()
-        assert abs(r0 - np.abs(rhs_0).max()) <= 1e-10 * np.abs(rhs_0).max()
+        rhs0 = oracle.build_rhs(C, F0, bt, np.zeros_like(expect), b, dx)
+        assert np.abs(rhs - rhs0).max() <= 1e-12 * np.abs(rhs0).max()
+        res_g = oracle.restrict(rhs0 - oracle.fapply(C, bt, expect, dx))
+        assert abs(rg - np.linalg.norm(res_g)) <= 1e-10 * np.linalg.norm(res_g)
+        assert abs(r0 - np.linalg.norm(oracle.restrict(rhs0))) <= 1e-10 * np.linalg.norm(oracle.restrict(rhs0))
         if used:
             assert rg <= r0
             assert np.abs(u - expect).max() <= 1e-12 * max(np.abs(expect).max(), 1e-300)
         else:
             assert rg > r0
             assert not np.any(u)
+        # the linear solve from the guess reaches the Newton-from-zero answer
+        op.SetOpts(agb.default_opts(solver="fgmres"))
+        x = u.copy()
+        agb.Linear(op).solve(x, rhs, 1e-10, 0.0)
+        u0 = np.zeros((3, n, n, n))
+        agb.Newton(op).solve(u0, b, F0, tol_rel=1e-10, tol_abs=0.0)
+        assert np.abs(x - u0).max() <= 1e-5 * np.abs(u0).max()
