@@ -179,19 +179,27 @@ __global__ void __launch_bounds__(NT, 2)
     issue_u(k0);
     issue_u(k0 + 1);
 
+    // one thread waits for the stiffness planes (the block barrier then
+    // orders everyone's reads after the completed copies); no thread polls
+    // while others compute
+    if (tid == 0) {
+        const bool ok = mbar_wait(bar_u32 + 8u * ((k0 - 1) % CS), parity(k0 - 1)) &&
+                        mbar_wait(bar_u32 + 8u * (k0 % CS), parity(k0)) &&
+                        mbar_wait(bar_u32 + 8u * ((k0 + 1) % CS), parity(k0 + 1));
+        if (!ok) {
+            abort_flag = 1;
+            if (err) atomicExch(err, 1);
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
     float Cp[NC];
-    bool ok = mbar_wait(bar_u32 + 8u * ((k0 - 1) % CS), parity(k0 - 1));
-    ok = ok && mbar_wait(bar_u32 + 8u * (k0 % CS), parity(k0));
     {
         const float* c = cslot(k0 - 1);
 #pragma unroll
         for (int e = 0; e < NC; e++) Cp[e] = c[e * CEL];
     }
-    if (!ok) {
-        abort_flag = 1;
-        if (err) atomicExch(err, 1);
-    }
-    cp_async_wait_all();
+    // the first step reloads the slot of plane k0 - 1: everyone has read it
     __syncthreads();
 
     // right-hand side and diagonal of the own column, loaded one plane ahead
@@ -221,9 +229,8 @@ __global__ void __launch_bounds__(NT, 2)
         const int64_t id = i + sy * j + sz * (int64_t)k;
         float bn[3] = {0.f, 0.f, 0.f}, dn[3] = {1.f, 1.f, 1.f};
         load_bd(k + 1, bn, dn);
-        const bool okn = mbar_wait(bar_u32 + 8u * ((k + 1) % CS), parity(k + 1));
         const float* cc = cslot(k);
-        if (col && okn) {
+        if (col) {
             const float* cn = cslot(k + 1);
             const int o = (ty + 1) * UHX + (tx + 1);
             const float* u0 = Us + (k % US) * UPL + o;
@@ -261,11 +268,11 @@ __global__ void __launch_bounds__(NT, 2)
             bq[c] = bn[c];
             dq[c] = dn[c];
         }
-        if (!okn) {
+        cp_async_wait_all();
+        if (tid == 0 && k + 2 <= k1 && !mbar_wait(bar_u32 + 8u * ((k + 2) % CS), parity(k + 2))) {
             abort_flag = 1;
             if (err) atomicExch(err, 1);
         }
-        cp_async_wait_all();
         __syncthreads();
     }
     if (abort_flag && tid == 0) {

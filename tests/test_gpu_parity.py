@@ -422,3 +422,21 @@ def test_mixed_matches_fp64_129(agb):
             assert rep["status"] == 0
             sols.append(u)
     assert rel(sols[1], sols[0]) <= 1e-7
+
+
+def test_zmarch_tma_repeatable_at_scale(agb):
+    """The TMA-staged sweeps at 129^3 (640 blocks, 10 z-chunks) against the
+    one-thread-per-node kernels, five times over: a missing wait or barrier
+    in the staging pipeline shows up as a run-to-run difference or a wrong
+    plane at a chunk boundary."""
+    C = np.ascontiguousarray(agb.synth.voronoi_cubic(129, 64, seed=11)[0])
+    bc = P.random_bc(13)
+    dx = 1.0 / 128
+    u = P.random_field((3, 129, 129, 129), 14).astype(np.float32)
+    with make_op(agb, C, bc, dx, fine_kernel=1) as op:
+        ref = op.Fapply_f32(u)
+    with make_op(agb, C, bc, dx, fine_kernel=0) as op:
+        outs = [op.Fapply_f32(u) for _ in range(5)]
+    for f in outs:
+        assert np.array_equal(f, outs[0])
+        assert rel(f, ref) <= 2e-6
