@@ -1311,9 +1311,11 @@ agb_status agb_linear_solve(agb_elastic* h, double* sol, const double* rhs, doub
     return st;
 }
 
-agb_status agb_newton_solve(agb_elastic* h, double* u, const double* b, const double* F0, int f0_ncomp,
-                            double tol_rel, double tol_abs, agb_solve_report* rep, int where) {
+agb_status agb_newton_solve_n(agb_elastic* h, double* u, const double* b, const double* F0, int f0_ncomp,
+                              double tol_rel, double tol_abs, int nriters, double nrtolerance, agb_solve_report* rep,
+                              double* relnorm, int where) {
     if (!h || !u || !b) return fail(AGB_BAD_ARG, "null argument");
+    if (nriters < 1) return fail(AGB_BAD_ARG, "nriters must be at least 1");
     if (!(f0_ncomp == 0 || f0_ncomp == 1 || f0_ncomp == 9) || (f0_ncomp && !F0))
         return fail(AGB_BAD_ARG, "f0_ncomp must be 0, 1 or 9 (with F0 given)");
     if (!h->model_set) return fail(AGB_NOT_READY, "model not set");
@@ -1326,17 +1328,31 @@ agb_status agb_newton_solve(agb_elastic* h, double* u, const double* b, const do
     if (f0_ncomp) TRY(dev_in(h, 3, F0, sizeof(double) * f0_ncomp * N, where, &dF));
     TRY(ensure_io(h, 2, 2 * bytes));
     double* rhs = h->io[2];
-    double* du_inc = h->io[2] + 3 * N;
-    TRY(build_rhs_dev(h, (const double*)du, (const double*)db, (const double*)dF, f0_ncomp, rhs));
-    CK(cudaMemsetAsync(du_inc, 0, bytes, h->stream));
-    agb_status st = solve_dev(h, du_inc, rhs, tol_rel, tol_abs, rep, true);
-    if (st != AGB_OK && st != AGB_NOT_CONVERGED) return st;
-    CK(launch_axpy(1.0, du_inc, (double*)du, 3 * N, h->stream));
-    h->launches++;
+    double* dsol = h->io[2] + 3 * N;
+    CK(cudaMemsetAsync(dsol, 0, bytes, h->stream));
+    agb_status st = AGB_OK;
+    double rn = 0.0;
+    for (int it = 0; it < nriters; it++) {
+        TRY(build_rhs_dev(h, (const double*)du, (const double*)db, (const double*)dF, f0_ncomp, rhs));
+        st = solve_dev(h, dsol, rhs, tol_rel, tol_abs, rep, it == 0);
+        if (st != AGB_OK && st != AGB_NOT_CONVERGED) return st;
+        double n2[2];
+        TRY(vec_norms(h, dsol, 3 * N, n2));
+        rn = n2[0];
+        CK(launch_axpy(1.0, dsol, (double*)du, 3 * N, h->stream));
+        h->launches++;
+        if (rn < nrtolerance) break;
+    }
+    if (relnorm) *relnorm = rn;
     agb_status s2 = finish_out(h, u, du, bytes, where);
     if (s2 != AGB_OK) return s2;
     if (rep) rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return st;
+}
+
+agb_status agb_newton_solve(agb_elastic* h, double* u, const double* b, const double* F0, int f0_ncomp,
+                            double tol_rel, double tol_abs, agb_solve_report* rep, int where) {
+    return agb_newton_solve_n(h, u, b, F0, f0_ncomp, tol_rel, tol_abs, 1, 0.0, rep, nullptr, where);
 }
 
 agb_status agb_elastic_learned_guess(agb_elastic* h, agb_unet* net, const double* b, const double* F0, int f0_ncomp,

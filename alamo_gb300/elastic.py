@@ -313,14 +313,34 @@ class Linear:
 
 
 class Newton(Linear):
-    """Solver::Nonlocal::Newton with nriters = 1 for linear models."""
+    """Solver::Nonlocal::Newton for linear models (setNRIters /
+    nrtolerance of the reference; nriters = 1 by default)."""
+
+    def __init__(self, op, nriters=1, nrtolerance=0.0):
+        super().__init__(op)
+        self.nriters = int(nriters)
+        self.nrtolerance = float(nrtolerance)
 
     def solve(self, u, b, F0=None, tol_rel=1e-8, tol_abs=0.0, allow_not_converged=False):
+        """Returns the last linear solve's report as a dict, plus "relnorm"
+        (max |increment| of the last iteration) when nriters > 1."""
         rep = L.SolveReport()
         pF, nF, wF = Elastic._f0(F0)
         pu, wu = _arg(u)
         pb, wb = _arg(b)
-        st = L.lib().agb_newton_solve(self.op.h, pu, pb, pF, nF, ctypes.c_double(tol_rel), ctypes.c_double(tol_abs),
-                                      ctypes.byref(rep), _same_where(wu, wb, wF))
+        where = _same_where(wu, wb, wF)
+        if self.nriters == 1:
+            st = L.lib().agb_newton_solve(self.op.h, pu, pb, pF, nF, ctypes.c_double(tol_rel),
+                                          ctypes.c_double(tol_abs), ctypes.byref(rep), where)
+            rn = None
+        else:
+            r = ctypes.c_double()
+            st = L.lib().agb_newton_solve_n(self.op.h, pu, pb, pF, nF, ctypes.c_double(tol_rel),
+                                            ctypes.c_double(tol_abs), self.nriters, ctypes.c_double(self.nrtolerance),
+                                            ctypes.byref(rep), ctypes.byref(r), where)
+            rn = r.value
         L.check(st, (L.AGB_OK, L.AGB_NOT_CONVERGED) if allow_not_converged else (L.AGB_OK,))
-        return rep.as_dict()
+        d = rep.as_dict()
+        if rn is not None:
+            d["relnorm"] = rn
+        return d

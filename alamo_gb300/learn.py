@@ -245,6 +245,9 @@ def _main():
     tr.add_argument("--lr", type=float, default=1e-3)
     tr.add_argument("--seed", type=int, default=1)
     tr.add_argument("--out", required=True)
+    pr = sub.add_parser("predict", help="time the network on one inclusion medium of its grid")
+    pr.add_argument("--weights", required=True)
+    pr.add_argument("--repeat", type=int, default=10)
     ev = sub.add_parser("evaluate")
     ev.add_argument("--weights", required=True)
     ev.add_argument("--n", type=int, default=129)
@@ -266,6 +269,20 @@ def _main():
         return
     net = UNet(65)
     net.load(a.weights)
+    if a.cmd == "predict":
+        C, F0, dx = inclusion_medium(65, np.random.default_rng(7))
+        f = torch.from_numpy(features_of(C, F0)).to(dev)
+        u = torch.empty_like(f)
+        ts = []
+        for _ in range(a.repeat):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            net.predict(DevicePtr(f.data_ptr()), DevicePtr(u.data_ptr()))
+            ts.append(time.perf_counter() - t0)
+        print(json.dumps({"grid": 65, "predict_ms_median": 1e3 * float(np.median(ts)),
+                          "predict_ms_first": 1e3 * ts[0]}))
+        net.close()
+        return
     rng = np.random.default_rng(a.seed)
     rows = []
     for k in range(a.count):

@@ -177,16 +177,23 @@ def cpu_sample(cfg, n_override, C, F0, bc, dx, cycles):
     rhs = O.build_rhs(C, F0, bt, u, b, dx)
     t_rhs = time.perf_counter() - t0
     sample_cycles = 6
-    _, rep, _ = O.solve(C, bt, rhs, dx, fixed_iter=sample_cycles)
+    x, rep, _ = O.solve(C, bt, rhs, dx, fixed_iter=sample_cycles)
     per_cycle = (rep.seconds - rep.setup_seconds) / sample_cycles
     setup = rep.setup_seconds + t_rhs
     est = setup + per_cycle * cycles
+    # one operator application at full size, median of three
+    fap = []
+    for _ in range(3):
+        t3 = time.perf_counter()
+        O.fapply(C, bt, x, dx)
+        fap.append(time.perf_counter() - t3)
     return {"value": est, "unit": "s", "cores": threads, "kind": "port",
             "sample": "oracle (C++ restatement of the reference CPU path, OpenMP) on %d host threads: RHS build + "
                       "set-up + %d fixed FP64 V-cycles at the full %d^3 size; solve time = set-up + "
                       "per-cycle time x %d cycles (the FP64 cycle count of this input to 1e-8)"
                       % (threads, sample_cycles, n, cycles),
-            "per_cycle_s": per_cycle, "setup_s": setup, "sample_wall_s": time.perf_counter() - t0}
+            "per_cycle_s": per_cycle, "setup_s": setup, "fapply_s": float(np.median(fap)),
+            "fapply_node_updates_per_s": float(n ** 3 / np.median(fap)), "sample_wall_s": time.perf_counter() - t0}
 
 
 def run_reference(args):

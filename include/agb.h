@@ -196,6 +196,15 @@ agb_status agb_linear_solve(agb_elastic* h, double* sol, const double* rhs, doub
  * at u, solves for the increment and adds it to u. */
 agb_status agb_newton_solve(agb_elastic* h, double* u, const double* b, const double* F0, int f0_ncomp,
                             double tol_rel, double tol_abs, agb_solve_report* rep, int where);
+/* Newton::solve with nriters iterations (Newton.H:279-358): each builds the
+ * right-hand side at the current u, solves for the increment starting from
+ * the previous increment (the reference keeps its correction field across
+ * iterations), adds it to u and stops when max |increment| < nrtolerance
+ * (the reference's absolute test).  *relnorm (may be NULL) = the last
+ * max |increment|; rep describes the last linear solve. */
+agb_status agb_newton_solve_n(agb_elastic* h, double* u, const double* b, const double* F0, int f0_ncomp,
+                              double tol_rel, double tol_abs, int nriters, double nrtolerance, agb_solve_report* rep,
+                              double* relnorm, int where);
 /* Stress / strain / energy after a solve (src/Integrator/Base/Mechanics.H:
  * 210-248, src/Operator/Elastic.cpp:426-603): stress = C (grad u - F0),
  * strain = sym grad u, 9 row-major values per node; energy = sigma:eps / 2.

@@ -440,3 +440,29 @@ def test_zmarch_tma_repeatable_at_scale(agb):
     for f in outs:
         assert np.array_equal(f, outs[0])
         assert rel(f, ref) <= 2e-6
+
+
+def test_newton_iterations_match_oracle_loop(agb, oracle):
+    """Newton::solve with nriters = 3 (Newton.H:319-355): right-hand side at
+    the current u, increment solved from the previous increment, u += it,
+    stop on max |increment| < nrtolerance -- the same loop on the oracle."""
+    C, F0, bc, dx = CASES["voronoi-mm"]()
+    n = C.shape[0]
+    bt, bv = bc.tables()
+    u0 = np.zeros((3, n, n, n))
+    b = oracle.bc_init(u0, bt, bv)
+    u = u0.copy()
+    dsol = np.zeros_like(u)
+    for it in range(3):
+        rhs = oracle.build_rhs(C, F0, bt, u, b, dx)
+        dsol, rep, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, x0=dsol)
+        u = u + dsol
+        rn_o = np.abs(dsol).max()
+    with make_op(agb, C, bc, dx) as op:
+        ug = u0.copy()
+        rep = agb.Newton(op, nriters=3, nrtolerance=0.0).solve(ug, b, F0, tol_rel=1e-10, tol_abs=0.0)
+    assert rel(ug, u) <= 1e-8
+    assert abs(rep["relnorm"] - rn_o) <= 1e-6 * max(rn_o, 1e-30)
+    # the later iterations correct the difference between the operator and
+    # the right-hand side's stress divergence (a few per mille of u here)
+    assert rn_o < 1e-2 * np.abs(u).max()
