@@ -47,6 +47,13 @@ template <typename T>
 cudaError_t launch_prolong_add(const T* crse, const LevelGeom<T>& Gc, T* fine, const LevelGeom<T>& Gf,
                                cudaStream_t s);
 
+// psi (Elastic::SetPsi / averageDownCoeffs, src/Operator/Elastic.cpp:118-137,
+// 839-905) in the ghosted layout of LevelGeom::psi: the fine level from the
+// caller's cells, and one coarsening
+cudaError_t launch_psi_embed(const double* cells, const LevelGeom<double>& G, double* psi, cudaStream_t s);
+cudaError_t launch_coarsen_psi(const double* pf, const LevelGeom<double>& Gf, double* pc, const LevelGeom<double>& Gc,
+                               cudaStream_t s);
+
 // layout and precision helpers
 cudaError_t launch_aos_to_soa(const double* aos, double* soa, int64_t N, int nc, cudaStream_t s);
 // (lambda, mu, F0) per node, SoA 3 x N: the isotropic entries or the Voigt

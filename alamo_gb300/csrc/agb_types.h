@@ -30,6 +30,13 @@ struct LevelGeom {
     T inv[3];        // 1 / dx    (one-sided first derivative)
     T i2[3];         // 1 / dx^2  (second derivative)
     T q[3];          // 0.25 / (dx_a dx_b) for the pairs xy, xz, yz
+    // psi of Operator::Elastic (void indicator, Elastic.cpp:191-192): cell
+    // field with one ghost layer, (nx+1)(ny+1)(nz+1) values, entry (a,b,c) =
+    // cell (a-1,b-1,c-1), strides psy = nx+1 and psz = (nx+1)(ny+1).
+    // nullptr when no psi is set.
+    const T* psi;
+    T psi_small;
+    int64_t psy, psz;
 };
 
 // index of the 21 major-minor entries by Voigt-pair (00,01,02,11,12,22) rows

@@ -69,6 +69,9 @@ struct Lev {
     T* Cpad = nullptr;
     CUtensorMap map{};
     bool tma = false;
+    // psi of this level (ghosted, LevelGeom::psi layout), owned; the FP64
+    // fine level uses the handle's psi_fine instead
+    T* psi = nullptr;
 };
 
 // Krylov space of the flexible GMRES: Arnoldi basis V (m+1 vectors), the
@@ -124,6 +127,10 @@ struct agb_elastic {
     double* io[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t io_cap[4] = {0, 0, 0, 0};
     double* dw = nullptr;  // 9N scratch of the Newton RHS
+    // psi (Elastic::SetPsi): ghosted fine-level field, m_psi_small
+    double* psi_fine = nullptr;
+    double psi_small = 1e-8;
+    bool psi_set = false;
     Krylov<double> K64;
     Krylov<float> K32;
     // dense direct bottom solve
@@ -205,6 +212,7 @@ void free_levels(std::vector<Lev<T>>& L) {
     for (auto& l : L) {
         cudaFree(l.C); cudaFree(l.diag); cudaFree(l.res); cudaFree(l.cor); cudaFree(l.rescor); cudaFree(l.tmp);
         cudaFree(l.Cpad);
+        cudaFree(l.psi);
     }
     L.clear();
 }
@@ -256,6 +264,10 @@ agb_status alloc_levels64(agb_elastic* h) {
         h->partials = nullptr;
         CK(cudaMalloc(&h->partials, sizeof(double) * 2 * maxblocks));
         h->partials_cap = maxblocks;
+    }
+    if (h->psi_set) {
+        h->L64[0].G.psi = h->psi_fine;
+        h->L64[0].G.psi_small = h->psi_small;
     }
     const Lev<double>& b = h->L64.back();
     cudaFree(h->bottom_work);
@@ -353,10 +365,23 @@ agb_status build_f32(agb_elastic* h) {
     for (int l = 0; l < nl; l++) {
         Lev<float>& v = h->L32[l];
         CK(launch_to_float(h->L64[l].C, v.C, h->L64[l].G.N * h->nc, 1.0, h->stream));
+        h->launches++;
+        if (h->psi_set) {
+            const int64_t np = v.G.psz * (v.G.nz + 1);
+            if (!v.psi) CK(cudaMalloc(&v.psi, sizeof(float) * np));
+            CK(launch_to_float(h->L64[l].G.psi, v.psi, np, 1.0, h->stream));
+            h->launches++;
+            v.G.psi = v.psi;
+            v.G.psi_small = (float)h->psi_small;
+        } else {
+            v.G.psi = nullptr;
+        }
         CK(launch_diagonal<float>(h->sym, v.C, v.G, h->bc, v.diag, h->stream));
-        h->launches += 2;
+        h->launches++;
         const LevelGeom<float>& G = v.G;
-        const bool want = h->opts.fine_kernel == 0 && G.N >= TMA_MIN_NODES && zmarch_tma_supported(G.nx, G.ny, G.nz);
+        // the z-marching kernels carry no psi terms: psi runs on the per-node ones
+        const bool want = h->opts.fine_kernel == 0 && !h->psi_set && G.N >= TMA_MIN_NODES &&
+                          zmarch_tma_supported(G.nx, G.ny, G.nz);
         if (!want) {
             cudaFree(v.Cpad);
             v.Cpad = nullptr;
@@ -390,6 +415,24 @@ agb_status prepare(agb_elastic* h) {
     for (int l = 1; l < nl; l++) {
         CK(launch_restrict_C(h->L64[l - 1].C, h->L64[l - 1].G, h->L64[l].C, h->L64[l].G, h->nc, h->stream));
         h->launches++;
+    }
+    // psi on every level (Elastic::averageDownCoeffsSameAmrLevel,
+    // src/Operator/Elastic.cpp:839-905), before the diagonal that uses it
+    for (int l = 0; l < nl; l++) {
+        Lev<double>& v = h->L64[l];
+        if (!h->psi_set) {
+            v.G.psi = nullptr;
+            continue;
+        }
+        if (l == 0) {
+            v.G.psi = h->psi_fine;
+        } else {
+            if (!v.psi) CK(cudaMalloc(&v.psi, sizeof(double) * v.G.psz * (v.G.nz + 1)));
+            CK(launch_coarsen_psi(h->L64[l - 1].G.psi, h->L64[l - 1].G, v.psi, v.G, h->stream));
+            h->launches++;
+            v.G.psi = v.psi;
+        }
+        v.G.psi_small = h->psi_small;
     }
     for (int l = 0; l < nl; l++) {
         CK(launch_diagonal<double>(h->sym, h->L64[l].C, h->L64[l].G, h->bc, h->L64[l].diag, h->stream));
@@ -427,6 +470,7 @@ template <typename T>
 bool use_zm(const agb_elastic*, const Lev<T>&, int) { return false; }
 template <>
 bool use_zm<float>(const agb_elastic* h, const Lev<float>& v, int l) {
+    if (h->psi_set) return false;
     return h->opts.fine_kernel == 0 ? v.tma : (h->opts.fine_kernel == 2 && l == 0);
 }
 
@@ -976,6 +1020,7 @@ agb_status agb_elastic_destroy(agb_elastic* h) {
     cudaFree(h->bottom_info);
     cudaFree(h->bcval_dev);
     cudaFree(h->dw);
+    cudaFree(h->psi_fine);
     h->K64.release();
     h->K32.release();
     drop_bottom_graph(h);
@@ -1080,6 +1125,41 @@ agb_status agb_elastic_set_bc(agb_elastic* h, const int* type, const double* val
 agb_status agb_elastic_prepare(agb_elastic* h) {
     if (!h) return fail(AGB_BAD_ARG, "null handle");
     return prepare(h);
+}
+
+agb_status agb_elastic_set_psi(agb_elastic* h, const double* psi, double small, int where) {
+    if (!h) return fail(AGB_BAD_ARG, "null handle");
+    if (!psi) {
+        h->psi_set = false;
+        for (auto& v : h->L64) v.G.psi = nullptr;
+        for (auto& v : h->L32) v.G.psi = nullptr;
+    } else {
+        if (!(small >= 0.0 && small < 1.0)) return fail(AGB_BAD_ARG, "psi_small must be in [0, 1)");
+        const LevelGeom<double>& G = h->L64[0].G;
+        const size_t cells = (size_t)(G.nx - 1) * (G.ny - 1) * (G.nz - 1);
+        if (!h->psi_fine) CK(cudaMalloc(&h->psi_fine, sizeof(double) * G.psz * (G.nz + 1)));
+        if (where == AGB_MEM_HOST) {
+            double* tmp = nullptr;
+            CK(cudaMallocAsync((void**)&tmp, sizeof(double) * cells, h->stream));
+            CK(cudaMemcpyAsync(tmp, psi, sizeof(double) * cells, cudaMemcpyHostToDevice, h->stream));
+            CK(launch_psi_embed(tmp, G, h->psi_fine, h->stream));
+            CK(cudaFreeAsync(tmp, h->stream));
+        } else if (where == AGB_MEM_DEVICE) {
+            CK(launch_psi_embed(psi, G, h->psi_fine, h->stream));
+        } else {
+            return fail(AGB_BAD_ARG, "where must be AGB_MEM_HOST or AGB_MEM_DEVICE");
+        }
+        h->launches++;
+        CK(cudaStreamSynchronize(h->stream));
+        h->psi_set = true;
+        h->psi_small = small;
+        h->L64[0].G.psi = h->psi_fine;
+        h->L64[0].G.psi_small = small;
+    }
+    drop_bottom_graph(h);  // its kernels hold the coarsest level's geometry
+    h->prepared = false;
+    h->have_f32 = false;
+    return AGB_OK;
 }
 
 agb_status agb_elastic_num_levels(agb_elastic* h, int* nl) {

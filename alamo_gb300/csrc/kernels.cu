@@ -31,6 +31,10 @@ LevelGeom<T> make_geom(int nx, int ny, int nz, const double dx[3]) {
     G.q[0] = T(0.25 / (dx[0] * dx[1]));
     G.q[1] = T(0.25 / (dx[0] * dx[2]));
     G.q[2] = T(0.25 / (dx[1] * dx[2]));
+    G.psi = nullptr;
+    G.psi_small = T(0);
+    G.psy = nx + 1;
+    G.psz = (int64_t)(nx + 1) * (ny + 1);
     return G;
 }
 template LevelGeom<double> make_geom<double>(int, int, int, const double*);
@@ -44,13 +48,13 @@ template LevelGeom<float> make_geom<float>(int, int, int, const double*);
     const int64_t id = i + G.sy * j + G.sz * k;
 
 // ---------------------------------------------------------------- Fapply
-template <typename T, int SYM>
+template <typename T, int SYM, bool PSI>
 __global__ void __launch_bounds__(256) k_fapply(const T* __restrict__ u, const T* __restrict__ C, LevelGeom<T> G,
                                                 BcTable bc, T* __restrict__ f) {
     AGB_NODE_INDEX
     if (!live) return;
     T r[3];
-    apply_node<T, SYM>(u, C, G, bc, i, j, k, id, r);
+    apply_node<T, SYM, PSI>(u, C, G, bc, i, j, k, id, r);
     f[id] = r[0];
     f[G.N + id] = r[1];
     f[2 * G.N + id] = r[2];
@@ -60,8 +64,13 @@ template <typename T>
 cudaError_t launch_fapply(int sym, const T* u, const T* C, const LevelGeom<T>& G, const BcTable& bc, T* f,
                           cudaStream_t s) {
     dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
-    if (sym == SYM_ISO) k_fapply<T, SYM_ISO><<<grd, blk, 0, s>>>(u, C, G, bc, f);
-    else k_fapply<T, SYM_MM><<<grd, blk, 0, s>>>(u, C, G, bc, f);
+    if (G.psi) {
+        if (sym == SYM_ISO) k_fapply<T, SYM_ISO, true><<<grd, blk, 0, s>>>(u, C, G, bc, f);
+        else k_fapply<T, SYM_MM, true><<<grd, blk, 0, s>>>(u, C, G, bc, f);
+    } else {
+        if (sym == SYM_ISO) k_fapply<T, SYM_ISO, false><<<grd, blk, 0, s>>>(u, C, G, bc, f);
+        else k_fapply<T, SYM_MM, false><<<grd, blk, 0, s>>>(u, C, G, bc, f);
+    }
     return cudaGetLastError();
 }
 template cudaError_t launch_fapply<double>(int, const double*, const double*, const LevelGeom<double>&, const BcTable&,
@@ -97,14 +106,14 @@ template cudaError_t launch_diagonal<float>(int, const float*, const LevelGeom<f
 // One damped-Jacobi sweep of Operator<Grid::Node>::Fsmooth
 // (src/Operator/Operator.cpp:109-146) fused with the operator application:
 // Ax is never written to memory.
-template <typename T, int SYM>
+template <typename T, int SYM, bool PSI>
 __global__ void __launch_bounds__(256) k_jacobi(const T* __restrict__ x, const T* __restrict__ b,
                                                 const T* __restrict__ dg, const T* __restrict__ C, LevelGeom<T> G,
                                                 BcTable bc, T omega, T* __restrict__ xo) {
     AGB_NODE_INDEX
     if (!live) return;
     T ax[3];
-    apply_node<T, SYM>(x, C, G, bc, i, j, k, id, ax);
+    apply_node<T, SYM, PSI>(x, C, G, bc, i, j, k, id, ax);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         const int64_t q = c * G.N + id;
@@ -136,8 +145,13 @@ cudaError_t launch_jacobi(int sym, const T* x, const T* b, const T* diag, const 
         return cudaGetLastError();
     }
     dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
-    if (sym == SYM_ISO) k_jacobi<T, SYM_ISO><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
-    else k_jacobi<T, SYM_MM><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
+    if (G.psi) {
+        if (sym == SYM_ISO) k_jacobi<T, SYM_ISO, true><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
+        else k_jacobi<T, SYM_MM, true><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
+    } else {
+        if (sym == SYM_ISO) k_jacobi<T, SYM_ISO, false><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
+        else k_jacobi<T, SYM_MM, false><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
+    }
     return cudaGetLastError();
 }
 template cudaError_t launch_jacobi<double>(int, const double*, const double*, const double*, const double*,
@@ -172,7 +186,7 @@ __device__ __forceinline__ void block_max_sum(double& mx, double& sm, double* ou
     }
 }
 
-template <typename T, int SYM>
+template <typename T, int SYM, bool PSI>
 __global__ void __launch_bounds__(256) k_residual(const T* __restrict__ x, const T* __restrict__ b,
                                                   const T* __restrict__ C, LevelGeom<T> G, BcTable bc,
                                                   T* __restrict__ r, double* __restrict__ partials) {
@@ -180,7 +194,7 @@ __global__ void __launch_bounds__(256) k_residual(const T* __restrict__ x, const
     double mx = 0.0, sm = 0.0;
     if (live) {
         T ax[3];
-        apply_node<T, SYM>(x, C, G, bc, i, j, k, id, ax);
+        apply_node<T, SYM, PSI>(x, C, G, bc, i, j, k, id, ax);
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             const int64_t q = c * G.N + id;
@@ -207,8 +221,13 @@ cudaError_t launch_residual(int sym, const T* x, const T* b, const T* C, const L
                             T* r, double* partials, int* nblocks_out, cudaStream_t s) {
     dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
     if (nblocks_out) *nblocks_out = (int)(grd.x * grd.y * grd.z);
-    if (sym == SYM_ISO) k_residual<T, SYM_ISO><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
-    else k_residual<T, SYM_MM><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
+    if (G.psi) {
+        if (sym == SYM_ISO) k_residual<T, SYM_ISO, true><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
+        else k_residual<T, SYM_MM, true><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
+    } else {
+        if (sym == SYM_ISO) k_residual<T, SYM_ISO, false><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
+        else k_residual<T, SYM_MM, false><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
+    }
     return cudaGetLastError();
 }
 template cudaError_t launch_residual<double>(int, const double*, const double*, const double*,
@@ -558,6 +577,15 @@ __global__ void __launch_bounds__(256) k_rhs(const double* __restrict__ u, const
             }
             ret[c] = acc;
         }
+        if (G.psi) {
+            // Newton.H:255-261: div(dw) avg8(psi) + dw grad psi (no psi_small)
+            double gp[3];
+            const double avg = psi_node<double>(G, i, j, k, gp);
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+                ret[c] = ret[c] * avg + (dw[(c * 3 + 0) * N + id] * gp[0] + dw[(c * 3 + 1) * N + id] * gp[1] +
+                                         dw[(c * 3 + 2) * N + id] * gp[2]);
+        }
     }
 #pragma unroll
     for (int c = 0; c < 3; c++) rhs[c * N + id] = b[c * N + id] - ret[c];
@@ -572,6 +600,77 @@ cudaError_t launch_build_rhs(int sym, const double* u, const double* b, const do
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_rhs<<<grd, blk, 0, s>>>(u, b, dw, G, bc, rhs);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- psi
+// Ghosted psi of the fine level from the caller's (nx-1)(ny-1)(nz-1) cells;
+// ghost entries 1.0 (the reference's define-time fill, Elastic.cpp:49-52).
+__global__ void k_psi_embed(const double* __restrict__ cells, LevelGeom<double> G, double* __restrict__ psi) {
+    const int64_t tot = G.psz * (G.nz + 1);
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+        const int a = (int)(q % G.psy);
+        const int b = (int)((q / G.psy) % (G.ny + 1));
+        const int c = (int)(q / G.psz);
+        const bool ghost = a == 0 || b == 0 || c == 0 || a == G.nx || b == G.ny || c == G.nz;
+        psi[q] = ghost ? 1.0 : cells[(a - 1) + (int64_t)(G.nx - 1) * ((b - 1) + (int64_t)(G.ny - 1) * (c - 1))];
+    }
+}
+
+cudaError_t launch_psi_embed(const double* cells, const LevelGeom<double>& G, double* psi, cudaStream_t s) {
+    k_psi_embed<<<flat_blocks(G.psz * (G.nz + 1)), 256, 0, s>>>(cells, G, psi);
+    return cudaGetLastError();
+}
+
+// Coarse-level psi (Elastic.cpp:839-905): full weighting around fine cell
+// (2I, 2J, 2K).  The boundary cases compare the cell index against the node
+// domain's bounds, so only index 0 takes the face, edge and corner forms;
+// the last cell keeps the interior form (its fine neighbours 2I+1 are in the
+// domain).  Ghost entries 1.0.
+__global__ void k_coarsen_psi(const double* __restrict__ pf, LevelGeom<double> Gf, double* __restrict__ pc,
+                              LevelGeom<double> Gc) {
+    const int64_t tot = Gc.psz * (Gc.nz + 1);
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+        const int a = (int)(q % Gc.psy);
+        const int b = (int)((q / Gc.psy) % (Gc.ny + 1));
+        const int c = (int)(q / Gc.psz);
+        if (a == 0 || b == 0 || c == 0 || a == Gc.nx || b == Gc.ny || c == Gc.nz) {
+            pc[q] = 1.0;
+            continue;
+        }
+        const int I = a - 1, J = b - 1, K = c - 1;
+        const double* base = pf + (2 * I + 1) + Gf.psy * (2 * J + 1) + Gf.psz * (2 * K + 1);
+        const int64_t py = Gf.psy, pz = Gf.psz;
+        auto F = [&](int x, int y, int z) { return base[x + py * y + pz * z]; };
+        const bool xi = I == 0, yj = J == 0, zk = K == 0;
+        double v;
+        if (xi && yj && zk) v = F(0, 0, 0);
+        else if (yj && zk) v = F(-1, 0, 0) * 0.25 + F(0, 0, 0) * 0.5 + F(1, 0, 0) * 0.25;
+        else if (zk && xi) v = F(0, -1, 0) * 0.25 + F(0, 0, 0) * 0.5 + F(0, 1, 0) * 0.25;
+        else if (xi && yj) v = F(0, 0, -1) * 0.25 + F(0, 0, 0) * 0.5 + F(0, 0, 1) * 0.25;
+        else if (xi)
+            v = (F(0, -1, -1) + F(0, 0, -1) * 2.0 + F(0, 1, -1) + F(0, -1, 0) * 2.0 + F(0, 0, 0) * 4.0 +
+                 F(0, 1, 0) * 2.0 + F(0, -1, 1) + F(0, 0, 1) * 2.0 + F(0, 1, 1)) / 16.0;
+        else if (yj)
+            v = (F(-1, 0, -1) + F(-1, 0, 0) * 2.0 + F(-1, 0, 1) + F(0, 0, -1) * 2.0 + F(0, 0, 0) * 4.0 +
+                 F(0, 0, 1) * 2.0 + F(1, 0, -1) + F(1, 0, 0) * 2.0 + F(1, 0, 1)) / 16.0;
+        else if (zk)
+            v = (F(-1, -1, 0) + F(0, -1, 0) * 2.0 + F(1, -1, 0) + F(-1, 0, 0) * 2.0 + F(0, 0, 0) * 4.0 +
+                 F(1, 0, 0) * 2.0 + F(-1, 1, 0) + F(0, 1, 0) * 2.0 + F(1, 1, 0)) / 16.0;
+        else
+            v = (F(-1, -1, -1) + F(-1, -1, 1) + F(-1, 1, -1) + F(-1, 1, 1) + F(1, -1, -1) + F(1, -1, 1) +
+                 F(1, 1, -1) + F(1, 1, 1)) / 64.0 +
+                (F(0, -1, -1) + F(0, -1, 1) + F(0, 1, -1) + F(0, 1, 1) + F(-1, 0, -1) + F(1, 0, -1) +
+                 F(-1, 0, 1) + F(1, 0, 1) + F(-1, -1, 0) + F(-1, 1, 0) + F(1, -1, 0) + F(1, 1, 0)) / 32.0 +
+                (F(-1, 0, 0) + F(0, -1, 0) + F(0, 0, -1) + F(1, 0, 0) + F(0, 1, 0) + F(0, 0, 1)) / 16.0 +
+                F(0, 0, 0) / 8.0;
+        pc[q] = v;
+    }
+}
+
+cudaError_t launch_coarsen_psi(const double* pf, const LevelGeom<double>& Gf, double* pc, const LevelGeom<double>& Gc,
+                               cudaStream_t s) {
+    k_coarsen_psi<<<flat_blocks(Gc.psz * (Gc.nz + 1)), 256, 0, s>>>(pf, Gf, pc, Gc);
     return cudaGetLastError();
 }
 

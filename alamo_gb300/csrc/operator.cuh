@@ -121,7 +121,7 @@ __device__ __forceinline__ void grad_at(const T* __restrict__ u, const LevelGeom
 // the node.  Offsets that leave the grid are never requested.
 template <typename T, int SYM, typename UA, typename CF>
 __device__ __forceinline__ void boundary_rows(UA U, CF c, const LevelGeom<T>& G, const unsigned char* bt, int i,
-                                              int j, int k, T f[3]) {
+                                              int j, int k, T f[3], T pa = T(1)) {
     T g[3][3], s[3][3], n[3];
 #pragma unroll
     for (int p = 0; p < 3; p++) {
@@ -131,6 +131,11 @@ __device__ __forceinline__ void boundary_rows(UA U, CF c, const LevelGeom<T>& G,
         g[p][2] = d1_of(k < G.nz - 1 ? U(p, 0, 0, 1) : u0, u0, k > 0 ? U(p, 0, 0, -1) : u0, k, G.nz, G.h[2], G.inv[2]);
     }
     stress_of<T, SYM>(c, g, s);
+    // sigma psi_avg (Elastic.cpp:195); pa = 1 without psi leaves s unchanged
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) s[p][q] *= pa;
     const int cx = (i == 0) ? -1 : (i == G.nx - 1) ? 1 : 0;
     const int cy = (j == 0) ? -1 : (j == G.ny - 1) ? 1 : 0;
     const int cz = (k == 0) ? -1 : (k == G.nz - 1) ? 1 : 0;
@@ -142,10 +147,59 @@ __device__ __forceinline__ void boundary_rows(UA U, CF c, const LevelGeom<T>& G,
 // Apply the operator at a boundary node (i, j, k) reading global memory
 template <typename T, int SYM, typename CF>
 __device__ __forceinline__ void apply_boundary(const T* __restrict__ u, const LevelGeom<T>& G, const BcTable& bc, CF c,
-                                               int i, int j, int k, int64_t id, T f[3]) {
+                                               int i, int j, int k, int64_t id, T f[3], T pa = T(1)) {
     const int64_t N = G.N, sy = G.sy, sz = G.sz;
     auto U = [&](int p, int a, int b, int cc) { return u[p * N + id + a + sy * b + sz * cc]; };
-    boundary_rows<T, SYM>(U, c, G, bc.t, i, j, k, f);
+    boundary_rows<T, SYM>(U, c, G, bc.t, i, j, k, f, pa);
+}
+
+// psi at node (i, j, k): the mean of its 8 cells in the order of
+// Numeric::Interpolate::CellToNodeAverage (src/Numeric/Stencil.H:1390-1405)
+// and, when gp is given, Numeric::CellGradientOnNode (src/Numeric/
+// Stencil.H:699-715).  Entry (i, j, k) of the ghosted field is cell
+// (i-1, j-1, k-1), so P(a, b, c) below is cell (i+a, j+b, k+c).
+template <typename T>
+__device__ __forceinline__ T psi_node(const LevelGeom<T>& G, int i, int j, int k, T* gp) {
+    const T* base = G.psi + (i + 1) + G.psy * (j + 1) + G.psz * (k + 1);
+    const int64_t py = G.psy, pz = G.psz;
+    auto P = [&](int a, int b, int c) { return base[a + py * b + pz * c]; };
+    const T p000 = P(0, 0, 0), p100 = P(-1, 0, 0), p010 = P(0, -1, 0), p110 = P(-1, -1, 0);
+    const T p001 = P(0, 0, -1), p101 = P(-1, 0, -1), p011 = P(0, -1, -1), p111 = P(-1, -1, -1);
+    if (gp) {
+        gp[0] = T(0.25) * (p000 - p100 + p010 - p110 + p001 - p101 + p011 - p111) * G.inv[0];
+        gp[1] = T(0.25) * (p000 - p010 + p100 - p110 + p001 - p011 + p101 - p111) * G.inv[1];
+        gp[2] = T(0.25) * (p000 - p001 + p100 - p101 + p010 - p011 + p110 - p111) * G.inv[2];
+    }
+    return (p000 + p100 + p010 + p110 + p001 + p101 + p011 + p111) * T(0.125);
+}
+
+// psi_avg = (1 - small) avg8(psi) + small (Elastic.cpp:191-192)
+template <typename T>
+__device__ __forceinline__ T psi_avg_of(const LevelGeom<T>& G, T avg) {
+    return (T(1) - G.psi_small) * avg + G.psi_small;
+}
+
+// Interior rows with psi (Elastic.cpp:243-260): f (the rows without psi)
+// becomes f psi_avg + (C grad u) grad psi (1 - small).
+template <typename T, int SYM>
+__device__ __forceinline__ void psi_interior(const T* __restrict__ u, const T* __restrict__ C,
+                                             const LevelGeom<T>& G, int i, int j, int k, int64_t id, T f[3]) {
+    T gp[3];
+    const T pa = psi_avg_of(G, psi_node(G, i, j, k, gp));
+    const T w = T(1) - G.psi_small;
+#pragma unroll
+    for (int q = 0; q < 3; q++) gp[q] *= w;
+    const int64_t N = G.N;
+    const int64_t off[3] = {1, G.sy, G.sz};
+    T g[3][3], s[3][3];
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) g[p][q] = (u[p * N + id + off[q]] - u[p * N + id - off[q]]) * G.h[q];
+    auto cf = [&](int a) { return C[a * N + id]; };
+    stress_of<T, SYM>(cf, g, s);
+#pragma unroll
+    for (int r = 0; r < 3; r++) f[r] = f[r] * pa + (s[r][0] * gp[0] + s[r][1] * gp[1] + s[r][2] * gp[2]);
 }
 
 // Interior-node arithmetic with the displacement and the stiffness read
@@ -249,17 +303,21 @@ __device__ __forceinline__ void apply_interior(const T* __restrict__ u, const T*
     interior_rows<T, SYM>(U, Cf, G, f);
 }
 
-// Apply the operator at any node.
-template <typename T, int SYM>
+// Apply the operator at any node.  PSI = false compiles the psi terms out
+// (the kernels instantiate both and pick by G.psi, so the common case keeps
+// its register budget).
+template <typename T, int SYM, bool PSI = true>
 __device__ __forceinline__ void apply_node(const T* __restrict__ u, const T* __restrict__ C, const LevelGeom<T>& G,
                                            const BcTable& bc, int i, int j, int k, int64_t id, T f[3]) {
     const bool bnd = (i == 0) | (j == 0) | (k == 0) | (i == G.nx - 1) | (j == G.ny - 1) | (k == G.nz - 1);
     if (bnd) {
         const int64_t N = G.N;
         auto cf = [&](int a) { return C[a * N + id]; };
-        apply_boundary<T, SYM>(u, G, bc, cf, i, j, k, id, f);
+        const T pa = (PSI && G.psi) ? psi_avg_of(G, psi_node<T>(G, i, j, k, nullptr)) : T(1);
+        apply_boundary<T, SYM>(u, G, bc, cf, i, j, k, id, f, pa);
     } else {
         apply_interior<T, SYM>(u, C, G, id, f);
+        if (PSI && G.psi) psi_interior<T, SYM>(u, C, G, i, j, k, id, f);
     }
 }
 
@@ -279,6 +337,7 @@ __device__ __forceinline__ void diag_node(const T* __restrict__ C, const LevelGe
         const int cz = (k == 0) ? -1 : (k == G.nz - 1) ? 1 : 0;
         T n[3];
         const int reg = boundary_region<T>(cx, cy, cz, n);
+        const T pa = G.psi ? psi_avg_of(G, psi_node<T>(G, i, j, k, nullptr)) : T(1);
 #pragma unroll
         for (int p = 0; p < 3; p++) {
             T g[3][3], s[3][3];
@@ -294,6 +353,10 @@ __device__ __forceinline__ void diag_node(const T* __restrict__ C, const LevelGe
                     g[a][d] = v;
                 }
             stress_of<T, SYM>(cf, g, s);
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int d = 0; d < 3; d++) s[a][d] *= pa;
             dg[p] = bc_component<T>(bc.t, reg, p, T(1), g, s, n);
         }
     } else {
@@ -311,6 +374,12 @@ __device__ __forceinline__ void diag_node(const T* __restrict__ C, const LevelGe
                 for (int l = 0; l < 3; l++) acc += cf(mm_ut(pair_of(p, l), pair_of(p, l))) * (T(-2) * G.i2[l]);
                 dg[p] = acc;
             }
+        }
+        // Elastic.cpp:363: the interior diagonal times psi_avg
+        if (G.psi) {
+            const T pa = psi_avg_of(G, psi_node<T>(G, i, j, k, nullptr));
+#pragma unroll
+            for (int p = 0; p < 3; p++) dg[p] *= pa;
         }
     }
 }

@@ -130,6 +130,22 @@ class Elastic:
         L.check(L.lib().agb_elastic_set_bc(self.h, t.ctypes.data_as(ctypes.c_void_p),
                                            v.ctypes.data_as(ctypes.c_void_p)))
 
+    def SetPsi(self, psi, small=1e-8):
+        """Elastic::SetPsi (src/Operator/Elastic.cpp:118-137): psi is the
+        (nz-1, ny-1, nx-1) cell field of the void indicator; None clears it.
+        small is m_psi_small."""
+        if psi is None:
+            L.check(L.lib().agb_elastic_set_psi(self.h, None, ctypes.c_double(0.0), L.MEM_HOST))
+            self.psi = None
+            return
+        nx, ny, nz = self.n
+        shape = (nz - 1, ny - 1, nx - 1)
+        if isinstance(psi, np.ndarray) and tuple(psi.shape) != shape:
+            raise ValueError(f"psi must have the cell shape {shape}, got {tuple(psi.shape)}")
+        self.psi = psi
+        p, w = _arg(psi)
+        L.check(L.lib().agb_elastic_set_psi(self.h, p, ctypes.c_double(small), w))
+
     def SetOpts(self, opts):
         self.opts = opts
         L.check(L.lib().agb_elastic_set_opts(self.h, ctypes.byref(opts)))
@@ -320,6 +336,11 @@ class Newton(Linear):
         super().__init__(op)
         self.nriters = int(nriters)
         self.nrtolerance = float(nrtolerance)
+
+    def setPsi(self, psi, small=1e-8):
+        """Newton::setPsi (src/Solver/Nonlocal/Newton.H:46-49): the operator's
+        psi for the solves that follow (Elastic.SetPsi)."""
+        self.op.SetPsi(psi, small)
 
     def solve(self, u, b, F0=None, tol_rel=1e-8, tol_abs=0.0, allow_not_converged=False):
         """Returns the last linear solve's report as a dict, plus "relnorm"

@@ -141,6 +141,18 @@ agb_status agb_elastic_set_bc(agb_elastic* h, const int* type, const double* val
  * src/Operator/Elastic.cpp:746-836) and the diagonal of every level.  Called
  * implicitly by the solves after set_model / set_bc / set_opts. */
 agb_status agb_elastic_prepare(agb_elastic* h);
+/* Elastic::SetPsi (src/Operator/Elastic.cpp:118-137) and Newton::setPsi
+ * (src/Solver/Nonlocal/Newton.H:46-49): the void indicator psi as a CELL
+ * field, (nx-1)(ny-1)(nz-1) doubles, x fastest; small = m_psi_small
+ * (reference default 1e-8).  Fapply, Diagonal and Fsmooth then scale the
+ * stress by psi_avg = (1 - small) avg8(psi) + small and add
+ * (C grad u) grad psi (1 - small) on interior rows (Elastic.cpp:191-260,
+ * 341-363); coarse levels get the full-weighted psi of
+ * averageDownCoeffsSameAmrLevel (Elastic.cpp:839-905); the Newton RHS uses
+ * avg8(psi) div(dw) + dw grad psi (Newton.H:236-263).  Cells outside the
+ * domain read 1.0.  psi NULL clears it.  With psi set the FP32 levels use
+ * the per-node kernels (the z-marching ones carry no psi terms). */
+agb_status agb_elastic_set_psi(agb_elastic* h, const double* psi, double small, int where);
 agb_status agb_elastic_num_levels(agb_elastic* h, int* nlevels);
 agb_status agb_elastic_level_dims(agb_elastic* h, int level, int dims[3]);
 

@@ -81,6 +81,12 @@ const double S2 = 0.70710678118;
 struct Grid {
     int n[3];
     double dx[3];
+    // psi (SetPsi, Elastic.cpp:120-136): cell field stored with one ghost
+    // layer, (n0+1)(n1+1)(n2+1) values, entry (a,b,c) = cell (a-1,b-1,c-1);
+    // ghosts outside the domain keep the define-time fill 1.0
+    // (Elastic.cpp:49-52).  nullptr: psi not set.
+    const double* psi = nullptr;
+    double psi_small = 0.0;
     int64_t N() const { return (int64_t)n[0] * n[1] * n[2]; }
     int64_t id(int i, int j, int k) const { return i + (int64_t)n[0] * (j + (int64_t)n[1] * k); }
     bool boundary(int i, int j, int k) const {
@@ -241,9 +247,43 @@ inline void bc_row(const int* bc_type, int reg, const double nrm[3], const doubl
 // reference's m_uniform = true branch, Elastic.cpp:245).
 bool g_grad_c = true;
 
+// psi of the grid the per-call functions below operate on (orc_set_psi)
+const double* g_psi = nullptr;
+double g_psi_small = 0.0;
+
+inline int64_t psi_id(const Grid& g, int a, int b, int c) {
+    return a + (int64_t)(g.n[0] + 1) * (b + (int64_t)(g.n[1] + 1) * c);
+}
+// Numeric::Interpolate::CellToNodeAverage (Numeric/Stencil.H:1390-1405):
+// mean of the 8 cells at a node, summed in the reference's order
+inline double psi_cell_avg(const Grid& g, int i, int j, int k) {
+    auto P = [&](int a, int b, int c) { return g.psi[psi_id(g, i + 1 + a, j + 1 + b, k + 1 + c)]; };
+    return (P(0, 0, 0) + P(-1, 0, 0) + P(0, -1, 0) + P(-1, -1, 0) + P(0, 0, -1) + P(-1, 0, -1) + P(0, -1, -1) +
+            P(-1, -1, -1)) * 0.125;
+}
+// psi_avg of Fapply / Diagonal (Elastic.cpp:191-192)
+inline double psi_avg(const Grid& g, int i, int j, int k) {
+    if (!g.psi) return 1.0;
+    return (1.0 - g.psi_small) * psi_cell_avg(g, i, j, k) + g.psi_small;
+}
+// Numeric::CellGradientOnNode (Stencil.H:699-715)
+inline void psi_grad(const Grid& g, int i, int j, int k, double gp[3]) {
+    auto P = [&](int a, int b, int c) { return g.psi[psi_id(g, i + 1 + a, j + 1 + b, k + 1 + c)]; };
+    // cell (i + a, j + b, k + c) with a, b, c in {-1, 0}
+    gp[0] = 0.25 * (P(0, 0, 0) - P(-1, 0, 0) + P(0, -1, 0) - P(-1, -1, 0) + P(0, 0, -1) - P(-1, 0, -1) + P(0, -1, -1) -
+                    P(-1, -1, -1)) / g.dx[0];
+    gp[1] = 0.25 * (P(0, 0, 0) - P(0, -1, 0) + P(-1, 0, 0) - P(-1, -1, 0) + P(0, 0, -1) - P(0, -1, -1) + P(-1, 0, -1) -
+                    P(-1, -1, -1)) / g.dx[1];
+    gp[2] = 0.25 * (P(0, 0, 0) - P(0, 0, -1) + P(-1, 0, 0) - P(-1, 0, -1) + P(0, -1, 0) - P(0, -1, -1) + P(-1, -1, 0) -
+                    P(-1, -1, -1)) / g.dx[2];
+}
+
 // ---------------------------------------------------------------------------
 // Fapply at one node (Elastic.cpp:165-290; psi not set, m_uniform false)
 // ---------------------------------------------------------------------------
+void fapply_gradc(int sym, const Grid& g, const double* C, const double gu[3][3], double pa, int i, int j, int k,
+                  double f[3]);
+
 void fapply_node(int sym, const Grid& g, const double* C, const int* bct, const double* U, int i, int j, int k,
                  double f[3]) {
     const int64_t N = g.N();
@@ -261,10 +301,14 @@ void fapply_node(int sym, const Grid& g, const double* C, const int* bct, const 
     const double* c = C + id * nc;
     double sig[3][3];
     c_grad(sym, c, gu, sig);
+    const double pa = psi_avg(g, i, j, k);
     if (g.boundary(i, j, k)) {
         double nrm[3];
         const int reg = region(g, i, j, k, nrm);
-        bc_row(bct, reg, nrm, u, gu, sig, f);
+        double sp[3][3];
+        for (int p = 0; p < 3; p++)
+            for (int q = 0; q < 3; q++) sp[p][q] = g.psi ? sig[p][q] * pa : sig[p][q];
+        bc_row(bct, reg, nrm, u, gu, sp, f);
         return;
     }
     double b[3][3][3];
@@ -280,8 +324,22 @@ void fapply_node(int sym, const Grid& g, const double* C, const int* bct, const 
         b[p][2][1] = b[p][1][2];
     }
     c_hess(sym, c, b, f);
-    if (!g_grad_c) return;
-    // + sum_q (d_q C * gradu)_{:,q}: central differences of C (Elastic.cpp:245-254)
+    if (g.psi)
+        for (int r = 0; r < 3; r++) f[r] *= pa;
+    if (g_grad_c) fapply_gradc(sym, g, C, gu, pa, i, j, k, f);
+    if (g.psi) {
+        // + (C grad u) grad psi (1 - small) (Elastic.cpp:255-260)
+        double gp[3];
+        psi_grad(g, i, j, k, gp);
+        for (int q = 0; q < 3; q++) gp[q] *= (1.0 - g.psi_small);
+        for (int r = 0; r < 3; r++) f[r] += sig[r][0] * gp[0] + sig[r][1] * gp[1] + sig[r][2] * gp[2];
+    }
+}
+
+// + sum_q (d_q C * gradu)_{:,q} psi_avg: central differences of C (Elastic.cpp:245-254)
+void fapply_gradc(int sym, const Grid& g, const double* C, const double gu[3][3], double pa, int i, int j, int k,
+                  double f[3]) {
+    const int nc = nc_of(sym);
     double col[3][3];
     for (int q = 0; q < 3; q++) {
         const double* cp = C + g.id(i + E[q][0], j + E[q][1], k + E[q][2]) * nc;
@@ -292,7 +350,7 @@ void fapply_node(int sym, const Grid& g, const double* C, const int* bct, const 
         c_grad(sym, dc, gu, t);
         for (int r = 0; r < 3; r++) col[q][r] = t[r][q];
     }
-    for (int r = 0; r < 3; r++) f[r] += (col[0][r] + col[1][r]) + col[2][r];
+    for (int r = 0; r < 3; r++) f[r] += g.psi ? ((col[0][r] + col[1][r]) + col[2][r]) * pa : (col[0][r] + col[1][r]) + col[2][r];
 }
 
 // diagonal at one node (Elastic.cpp:321-373, Stencil.H:900-963)
@@ -313,6 +371,11 @@ void diag_node(int sym, const Grid& g, const double* C, const int* bct, int i, i
                 }
             double sig[3][3];
             c_grad(sym, c, gu, sig);
+            if (g.psi) {
+                const double pa = psi_avg(g, i, j, k);
+                for (int q = 0; q < 3; q++)
+                    for (int dd = 0; dd < 3; dd++) sig[q][dd] *= pa;
+            }
             double u[3] = {0, 0, 0};
             u[p] = 1.0;
             double nrm[3], f[3];
@@ -327,7 +390,7 @@ void diag_node(int sym, const Grid& g, const double* C, const int* bct, int i, i
                         b[q][l][jj] = (l == jj && p == q) ? -2.0 / g.dx[l] / g.dx[l] : 0.0;
             double f[3];
             c_hess(sym, c, b, f);
-            d[p] = 0.0 + f[p];
+            d[p] = 0.0 + (g.psi ? f[p] * psi_avg(g, i, j, k) : f[p]);
         }
     }
 }
@@ -463,6 +526,51 @@ void prolong_add(const Grid& gf, const Grid& gc, const double* crse, double* fin
                 }
 }
 
+// Coarse-level psi from the fine level (Elastic.cpp:839-905): full
+// weighting of the fine cells around coarse cell (I,J,K) = fine (2I,2J,2K).
+// The boundary cases compare the cell index against the NODE domain bounds,
+// so only index 0 (the low side) takes the face, edge and corner stencils;
+// the high side keeps the interior stencil.  Ghost entries stay at 1.0.
+void coarsen_psi(const Grid& gf, const Grid& gc, const double* pf, double* pc) {
+    const int64_t tot = (int64_t)(gc.n[0] + 1) * (gc.n[1] + 1) * (gc.n[2] + 1);
+    for (int64_t q = 0; q < tot; q++) pc[q] = 1.0;
+    auto F = [&](int i, int j, int k) { return pf[psi_id(gf, i + 1, j + 1, k + 1)]; };
+    for (int K = 0; K < gc.n[2] - 1; K++)
+        for (int J = 0; J < gc.n[1] - 1; J++)
+            for (int I = 0; I < gc.n[0] - 1; I++) {
+                const int i = 2 * I, j = 2 * J, k = 2 * K;
+                const bool xi = I == 0, yj = J == 0, zk = K == 0;
+                double v;
+                if (xi && yj && zk) v = F(i, j, k);
+                else if (yj && zk) v = F(i - 1, j, k) * 0.25 + F(i, j, k) * 0.5 + F(i + 1, j, k) * 0.25;
+                else if (zk && xi) v = F(i, j - 1, k) * 0.25 + F(i, j, k) * 0.5 + F(i, j + 1, k) * 0.25;
+                else if (xi && yj) v = F(i, j, k - 1) * 0.25 + F(i, j, k) * 0.5 + F(i, j, k + 1) * 0.25;
+                else if (xi)
+                    v = (F(i, j - 1, k - 1) + F(i, j, k - 1) * 2.0 + F(i, j + 1, k - 1) + F(i, j - 1, k) * 2.0 +
+                         F(i, j, k) * 4.0 + F(i, j + 1, k) * 2.0 + F(i, j - 1, k + 1) + F(i, j, k + 1) * 2.0 +
+                         F(i, j + 1, k + 1)) / 16.0;
+                else if (yj)
+                    v = (F(i - 1, j, k - 1) + F(i - 1, j, k) * 2.0 + F(i - 1, j, k + 1) + F(i, j, k - 1) * 2.0 +
+                         F(i, j, k) * 4.0 + F(i, j, k + 1) * 2.0 + F(i + 1, j, k - 1) + F(i + 1, j, k) * 2.0 +
+                         F(i + 1, j, k + 1)) / 16.0;
+                else if (zk)
+                    v = (F(i - 1, j - 1, k) + F(i, j - 1, k) * 2.0 + F(i + 1, j - 1, k) + F(i - 1, j, k) * 2.0 +
+                         F(i, j, k) * 4.0 + F(i + 1, j, k) * 2.0 + F(i - 1, j + 1, k) + F(i, j + 1, k) * 2.0 +
+                         F(i + 1, j + 1, k)) / 16.0;
+                else
+                    v = (F(i - 1, j - 1, k - 1) + F(i - 1, j - 1, k + 1) + F(i - 1, j + 1, k - 1) +
+                         F(i - 1, j + 1, k + 1) + F(i + 1, j - 1, k - 1) + F(i + 1, j - 1, k + 1) +
+                         F(i + 1, j + 1, k - 1) + F(i + 1, j + 1, k + 1)) / 64.0 +
+                        (F(i, j - 1, k - 1) + F(i, j - 1, k + 1) + F(i, j + 1, k - 1) + F(i, j + 1, k + 1) +
+                         F(i - 1, j, k - 1) + F(i + 1, j, k - 1) + F(i - 1, j, k + 1) + F(i + 1, j, k + 1) +
+                         F(i - 1, j - 1, k) + F(i - 1, j + 1, k) + F(i + 1, j - 1, k) + F(i + 1, j + 1, k)) / 32.0 +
+                        (F(i - 1, j, k) + F(i, j - 1, k) + F(i, j, k - 1) + F(i + 1, j, k) + F(i, j + 1, k) +
+                         F(i, j, k + 1)) / 16.0 +
+                        F(i, j, k) / 8.0;
+                pc[psi_id(gc, I + 1, J + 1, K + 1)] = v;
+            }
+}
+
 double norm_inf(const double* a, int64_t n) {
     double mx = 0.0;
 #pragma omp parallel for reduction(max : mx) schedule(static)
@@ -515,12 +623,34 @@ static Grid mkgrid(int nx, int ny, int nz, const double* dx) {
     Grid g;
     g.n[0] = nx; g.n[1] = ny; g.n[2] = nz;
     g.dx[0] = dx[0]; g.dx[1] = dx[1]; g.dx[2] = dx[2];
+    g.psi = g_psi;
+    g.psi_small = g_psi_small;
     return g;
 }
 
 // SetUniform (src/Operator/Elastic.H:104-107): uniform = 1 drops the
 // grad-C term of interior rows.
 void orc_set_uniform(int uniform) { g_grad_c = uniform == 0; }
+
+// psi for the calls that follow (Elastic::SetPsi, Elastic.cpp:118-137).
+// For a node grid nx*ny*nz, psi_ghost holds (nx+1)(ny+1)(nz+1) values: the
+// (nx-1)(ny-1)(nz-1) cells with one ghost layer on each side, x fastest,
+// entry (a,b,c) = cell (a-1,b-1,c-1).  The ghost entries must be 1.0 (the
+// reference fills its psi with 1.0 at define time and SetPsi copies only
+// the domain's cells).  nullptr clears psi.
+void orc_set_psi(const double* psi_ghost, double small) {
+    g_psi = psi_ghost;
+    g_psi_small = small;
+}
+
+// Coarse-level psi of one multigrid coarsening (Elastic.cpp:839-905); both
+// arrays in the ghosted layout of orc_set_psi (fine node grid nxf*nyf*nzf).
+void orc_coarsen_psi(int nxf, int nyf, int nzf, const double* pf, double* pc) {
+    const double one[3] = {1, 1, 1};
+    Grid gf = mkgrid(nxf, nyf, nzf, one);
+    Grid gc = mkgrid((nxf - 1) / 2 + 1, (nyf - 1) / 2 + 1, (nzf - 1) / 2 + 1, one);
+    coarsen_psi(gf, gc, pf, pc);
+}
 
 int orc_num_threads(void) {
 #ifdef _OPENMP
@@ -671,6 +801,15 @@ void orc_build_rhs(int sym, int nx, int ny, int nz, const double* dx, const doub
                 const int64_t im = g.id(i - E[d][0], j - E[d][1], k - E[d][2]);
                 for (int c = 0; c < 3; c++) ret[c] += (dw[ip * 9 + c * 3 + d] - dw[im * 9 + c * 3 + d]) / 2. / g.dx[d];
             }
+            if (g.psi) {
+                // Newton.H:255-261: raw cell average (no psi_small), dw grad psi
+                const double pa = psi_cell_avg(g, i, j, k);
+                double gp[3];
+                psi_grad(g, i, j, k, gp);
+                for (int c = 0; c < 3; c++)
+                    ret[c] = ret[c] * pa + dw[id * 9 + c * 3 + 0] * gp[0] + dw[id * 9 + c * 3 + 1] * gp[1] +
+                             dw[id * 9 + c * 3 + 2] * gp[2];
+            }
         }
         for (int d = 0; d < 3; d++) rhs[d * N + id] = b[d * N + id] - ret[d];
     });
@@ -776,8 +915,17 @@ namespace {
 
 struct Level {
     Grid g;
-    std::vector<double> C, diag, res, cor, rescor, tmp;
+    std::vector<double> C, diag, res, cor, rescor, tmp, psi;
 };
+
+// psi of level l > 0 coarsened from level l - 1 (prepareForSolve order:
+// averageDownCoeffs before Diagonal, Operator.cpp:253-259)
+void level_psi(Level& f, Level& c) {
+    if (!f.g.psi) { c.g.psi = nullptr; return; }
+    c.psi.assign((size_t)(c.g.n[0] + 1) * (c.g.n[1] + 1) * (c.g.n[2] + 1), 1.0);
+    coarsen_psi(f.g, c.g, f.g.psi, c.psi.data());
+    c.g.psi = c.psi.data();
+}
 
 struct Hier {
     int sym;
@@ -1002,7 +1150,10 @@ void orc_vcycle(int sym, int nx, int ny, int nz, const double* dx, const double*
         const int64_t N = v.g.N();
         v.C.resize(N * nc);
         if (l == 0) std::memcpy(v.C.data(), C, sizeof(double) * N * nc);
-        else restrict_generic(H.L[l - 1].g, v.g, H.L[l - 1].C.data(), v.C.data(), nc, 1, nc, 1, nc);
+        else {
+            restrict_generic(H.L[l - 1].g, v.g, H.L[l - 1].C.data(), v.C.data(), nc, 1, nc, 1, nc);
+            level_psi(H.L[l - 1], v);
+        }
         v.diag.resize(3 * N);
         diagonal(sym, v.g, v.C.data(), bc_type, v.diag.data());
         v.res.assign(3 * N, 0.0);
@@ -1043,6 +1194,7 @@ int orc_solve(int sym, int nx, int ny, int nz, const double* dx, const double* C
         else {
             Level& f = H.L[l - 1];
             restrict_generic(f.g, v.g, f.C.data(), v.C.data(), nc, 1, nc, 1, nc);
+            level_psi(f, v);
         }
         v.diag.resize(3 * N);
         diagonal(sym, v.g, v.C.data(), bc_type, v.diag.data());

@@ -275,3 +275,39 @@ def set_uniform(uniform):
     """Operator::Elastic::SetUniform: True drops the grad-C term."""
     lib().orc_set_uniform.restype = None
     lib().orc_set_uniform(int(bool(uniform)))
+
+
+_psi_keep = None
+
+
+def psi_ghosted(psi_cells):
+    """(nz-1, ny-1, nx-1) cell values -> (nz+1, ny+1, nx+1) with one ghost
+    layer of 1.0 on every side (the reference's define-time fill)."""
+    pc = np.asarray(psi_cells, dtype=np.float64)
+    g = np.ones(tuple(s + 2 for s in pc.shape))
+    g[1:-1, 1:-1, 1:-1] = pc
+    return g
+
+
+def set_psi(psi_cells, small=1e-8):
+    """Operator::Elastic::SetPsi for the calls that follow (None clears):
+    psi_cells is the (nz-1, ny-1, nx-1) cell field of a node grid."""
+    global _psi_keep
+    lib().orc_set_psi.restype = None
+    if psi_cells is None:
+        _psi_keep = None
+        lib().orc_set_psi(None, ctypes.c_double(0.0))
+        return
+    _psi_keep = np.ascontiguousarray(psi_ghosted(psi_cells))
+    lib().orc_set_psi(_p(_psi_keep), ctypes.c_double(small))
+
+
+def coarsen_psi(psi_cells):
+    """One multigrid coarsening of a cell psi field (Elastic.cpp:839-905):
+    (nz-1, ny-1, nx-1) fine cells -> coarse cells."""
+    g = np.ascontiguousarray(psi_ghosted(psi_cells))
+    nz, ny, nx = (s - 1 for s in g.shape)
+    out = np.empty(((nz - 1) // 2 + 2, (ny - 1) // 2 + 2, (nx - 1) // 2 + 2))
+    lib().orc_coarsen_psi.restype = None
+    lib().orc_coarsen_psi(nx, ny, nz, _p(g), _p(out))
+    return out[1:-1, 1:-1, 1:-1].copy()
