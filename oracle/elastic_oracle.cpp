@@ -29,6 +29,13 @@
 //   Newton RHS        src/Solver/Nonlocal/Newton.H:144-275
 //   stress/strain     src/Integrator/Base/Mechanics.H:210-248,
 //                     src/Operator/Elastic.cpp:426-603
+//   psi (void)        src/Operator/Elastic.cpp:118-137 (SetPsi), :191-260 and
+//                     :341-363 (psi_avg, grad psi terms), :839-905 (psi
+//                     coarsening); src/Numeric/Stencil.H:699-715
+//                     (CellGradientOnNode), :1390-1405 (CellToNodeAverage);
+//                     src/Solver/Nonlocal/Newton.H:236-263 (RHS).  Pinned
+//                     against numpy restatements (tests/test_psi.py); the
+//                     reference has no known-answer test for psi in 3D.
 //   V-cycle driver    behaviour of amrex::MLMG as configured by
 //                     src/Solver/Nonlocal/Linear.H:255-290 (AMReX itself is not
 //                     vendored in the reference: parity is unpinned at the MLMG
