@@ -59,7 +59,7 @@ class SolverOpts(ctypes.Structure):
         ("bottom_solver", ctypes.c_int),
         ("fine_kernel", ctypes.c_int),
         ("krylov_reorth", ctypes.c_int),
-        ("reserved_opts", ctypes.c_int),
+        ("tma_min_nodes", ctypes.c_int),
     ]
 
 

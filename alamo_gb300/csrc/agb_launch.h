@@ -127,8 +127,9 @@ namespace agb {
 // Dense direct bottom solve (nb = 3 N unknowns of the coarsest level):
 // work >= 4 nb^2 + 2 nb doubles, iwork >= 2 nb ints; flag[0] = 1 when a
 // pivot falls below 1e-12 max |diag| (written to tiny[0]): the level's
-// operator is singular to working precision.  Only kernels and a memset,
-// all argument values fixed, so the sequence can be captured in a graph.
+// operator is singular to working precision; flag[0] = 2 when the
+// elimination's grid barrier gave up waiting.  The elimination is one
+// cooperative launch (all columns, a bounded grid barrier per column).
 cudaError_t build_dense_inverse(int sym, const double* C, const double* diag, const LevelGeom<double>& G,
                                 const BcTable& bc, double* Ainv, double* work, int* iwork, int* flag, double* tiny,
                                 cudaStream_t s);

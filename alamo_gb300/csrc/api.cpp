@@ -137,10 +137,7 @@ struct agb_elastic {
     double* bot_inv = nullptr;
     int bot_nb = 0;
     bool bot_dense = false;
-    // its build (assembly + Gauss-Jordan, 2 nb + 4 launches) as a graph,
-    // captured once per level layout and boundary table, and its buffers
-    cudaGraphExec_t bot_exec = nullptr;
-    cudaStream_t cap_stream = nullptr;
+    // buffers of its build (assembly + one cooperative Gauss-Jordan launch)
     double* bot_work = nullptr;  // 4 nb^2 + 2 nb + 1 (threshold)
     int* bot_iwork = nullptr;    // 2 nb + 1 (flag)
     // profiling
@@ -233,10 +230,7 @@ int num_levels(const int n0[3], int max_coarsening_level) {
     return lev;
 }
 
-void drop_bottom_graph(agb_elastic* h);
-
 agb_status alloc_levels64(agb_elastic* h) {
-    drop_bottom_graph(h);  // its kernels hold pointers into the levels
     free_levels(h->L64);
     const int nl = num_levels(h->n, h->opts.max_coarsening_level);
     h->ldx.assign(3 * nl, 0.0);
@@ -298,17 +292,12 @@ agb_status alloc_levels32(agb_elastic* h) {
 // Explicit inverse of the coarsest level's operator for the direct bottom
 // solve; falls back to BiCGStab (bot_dense = false) when it is too large or
 // singular to working precision.
-void drop_bottom_graph(agb_elastic* h) {
-    if (h->bot_exec) cudaGraphExecDestroy(h->bot_exec);
-    h->bot_exec = nullptr;
-}
 
 agb_status build_bottom_dense(agb_elastic* h) {
     Lev<double>& b = h->L64.back();
     const int nb = (int)(3 * b.G.N);
     if (nb > 4000) return AGB_OK;
     if (h->bot_nb != nb) {
-        drop_bottom_graph(h);
         cudaFree(h->bot_inv);
         cudaFree(h->bot_work);
         cudaFree(h->bot_iwork);
@@ -323,27 +312,9 @@ agb_status build_bottom_dense(agb_elastic* h) {
     }
     int* flag = h->bot_iwork + 2 * nb;
     double* tiny = h->bot_work + 4 * (size_t)nb * nb + 2 * (size_t)nb;
-    if (!h->bot_exec) {
-        if (!h->cap_stream) CK(cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking));
-        CK(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
-        const cudaError_t e = build_dense_inverse(h->sym, b.C, b.diag, b.G, h->bc, h->bot_inv, h->bot_work,
-                                                  h->bot_iwork, flag, tiny, h->cap_stream);
-        cudaGraph_t g = nullptr;
-        const cudaError_t e2 = cudaStreamEndCapture(h->cap_stream, &g);
-        if (e != cudaSuccess || e2 != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            return fail(AGB_CUDA_ERROR, std::string("capture of the bottom-level inverse failed: ") +
-                                            cudaGetErrorString(e != cudaSuccess ? e : e2));
-        }
-        const cudaError_t e3 = cudaGraphInstantiate(&h->bot_exec, g, 0);
-        cudaGraphDestroy(g);
-        if (e3 != cudaSuccess) {
-            h->bot_exec = nullptr;
-            return fail(AGB_CUDA_ERROR, std::string("bottom-level graph: ") + cudaGetErrorString(e3));
-        }
-    }
-    CK(cudaGraphLaunch(h->bot_exec, h->stream));
-    h->launches += 2 * nb + 4;
+    CK(build_dense_inverse(h->sym, b.C, b.diag, b.G, h->bc, h->bot_inv, h->bot_work, h->bot_iwork, flag, tiny,
+                           h->stream));
+    h->launches += 5;
     int hflag = 0;
     CK(cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -355,7 +326,7 @@ agb_status build_bottom_dense(agb_elastic* h) {
 // levels at least this large (nodes) are swept by the TMA stencil kernels;
 // on smaller ones the per-node kernels, one launch instead of two, are
 // faster
-static constexpr int64_t TMA_MIN_NODES = 30000;
+static constexpr int64_t TMA_MIN_NODES = 30000;  // default of agb_solver_opts::tma_min_nodes
 
 // FP32 copies of every level's stiffness and diagonal; for the levels the
 // TMA stencil kernels sweep also the padded copy and its tensor map
@@ -380,7 +351,8 @@ agb_status build_f32(agb_elastic* h) {
         h->launches++;
         const LevelGeom<float>& G = v.G;
         // the z-marching kernels carry no psi terms: psi runs on the per-node ones
-        const bool want = h->opts.fine_kernel == 0 && !h->psi_set && G.N >= TMA_MIN_NODES &&
+        const int64_t min_nodes = h->opts.tma_min_nodes > 0 ? h->opts.tma_min_nodes : TMA_MIN_NODES;
+        const bool want = h->opts.fine_kernel == 0 && !h->psi_set && G.N >= min_nodes &&
                           zmarch_tma_supported(G.nx, G.ny, G.nz);
         if (!want) {
             cudaFree(v.Cpad);
@@ -948,7 +920,7 @@ agb_status agb_default_opts(agb_solver_opts* o) {
     o->bottom_solver = AGB_BOTTOM_BICGSTAB;
     o->fine_kernel = 0;
     o->krylov_reorth = 0;
-    o->reserved_opts = 0;
+    o->tma_min_nodes = 0;
     return AGB_OK;
 }
 
@@ -963,6 +935,7 @@ static agb_status check_opts(const agb_solver_opts* o) {
     if (o->bottom_solver < AGB_BOTTOM_BICGSTAB || o->bottom_solver > AGB_BOTTOM_SMOOTHER)
         return fail(AGB_BAD_ARG, "unknown bottom solver");
     if (o->fine_kernel < 0 || o->fine_kernel > 2) return fail(AGB_BAD_ARG, "fine_kernel must be 0, 1 or 2");
+    if (o->tma_min_nodes < 0) return fail(AGB_BAD_ARG, "tma_min_nodes must be >= 0");
     if (o->solver == AGB_SOLVER_FGMRES && (o->krylov_dim < 1 || o->krylov_dim > 39))
         return fail(AGB_BAD_ARG, "krylov_dim must lie in [1, 39]");
     if (o->solver == AGB_SOLVER_FGMRES && !(o->inner_tol > 0.0 && o->inner_tol < 1.0))
@@ -1023,11 +996,9 @@ agb_status agb_elastic_destroy(agb_elastic* h) {
     cudaFree(h->psi_fine);
     h->K64.release();
     h->K32.release();
-    drop_bottom_graph(h);
     cudaFree(h->bot_inv);
     cudaFree(h->bot_work);
     cudaFree(h->bot_iwork);
-    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     for (int s = 0; s < 4; s++) cudaFree(h->io[s]);
     for (auto e : h->ev_pool) cudaEventDestroy(e);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -1115,7 +1086,6 @@ agb_status agb_elastic_set_bc(agb_elastic* h, const int* type, const double* val
         if (type[q] < AGB_BC_DISPLACEMENT || type[q] > AGB_BC_NONE) return fail(AGB_BAD_ARG, "unknown BC type");
     }
     for (int q = 0; q < 78; q++) { h->bc.t[q] = (unsigned char)type[q]; h->bcval[q] = val[q]; }
-    drop_bottom_graph(h);  // the boundary table is a kernel argument in it
     h->bc_set = true;
     h->prepared = false;
     h->have_f32 = false;
@@ -1156,7 +1126,6 @@ agb_status agb_elastic_set_psi(agb_elastic* h, const double* psi, double small, 
         h->L64[0].G.psi = h->psi_fine;
         h->L64[0].G.psi_small = small;
     }
-    drop_bottom_graph(h);  // its kernels hold the coarsest level's geometry
     h->prepared = false;
     h->have_f32 = false;
     return AGB_OK;

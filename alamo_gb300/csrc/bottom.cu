@@ -245,72 +245,117 @@ __global__ void k_gj_init(const double* __restrict__ Acol, double* __restrict__ 
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nb; r += gridDim.x * blockDim.x) used[r] = 0;
 }
 
-// pivot of column k among the rows not used yet; prow = pivot row / pivot
-__global__ void __launch_bounds__(1024) k_gj_pivot(double* __restrict__ W, int nb, int k, int* __restrict__ used,
-                                                   int* __restrict__ perm, double* __restrict__ prow,
-                                                   int* __restrict__ flag, const double* __restrict__ tiny_p) {
-    const double tiny = tiny_p[0];
-    __shared__ double bv[32];
-    __shared__ int bi[32];
-    double best = -1.0;
-    int bidx = -1;
-    for (int r = threadIdx.x; r < nb; r += blockDim.x) {
-        if (used[r]) continue;
-        const double a = fabs(W[(int64_t)r * 2 * nb + k]);
-        if (a > best) { best = a; bidx = r; }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
-        if (ob > best || (ob == best && oi >= 0 && (bidx < 0 || oi < bidx))) { best = ob; bidx = oi; }
-    }
-    if ((threadIdx.x & 31) == 0) { bv[threadIdx.x >> 5] = best; bi[threadIdx.x >> 5] = bidx; }
+// Grid-wide barrier of the cooperative Gauss-Jordan kernel (all blocks are
+// co-resident under cudaLaunchCooperativeKernel).  bar[0] counts arrivals,
+// bar[1] is the generation.  The wait is bounded: past the limit the block
+// records flag = 2 and every block leaves the elimination loop.
+__device__ __forceinline__ bool gj_grid_barrier(unsigned* bar, unsigned nblocks, int* stop_sh, int* flag) {
     __syncthreads();
-    __shared__ int p_sh;
-    __shared__ double piv_sh;
-    if (threadIdx.x == 0) {
-        double b = -1.0;
-        int p = -1;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++)
-            if (bv[w] > b || (bv[w] == b && bi[w] >= 0 && (p < 0 || bi[w] < p))) { b = bv[w]; p = bi[w]; }
-        if (p < 0 || !(b > tiny)) { flag[0] = 1; p = (p < 0) ? 0 : p; }
-        used[p] = 1;
-        perm[k] = p;
-        p_sh = p;
-        piv_sh = W[(int64_t)p * 2 * nb + k];
+    if (threadIdx.x == 0 && !*stop_sh) {
+        __threadfence();
+        const unsigned gen = atomicAdd(&bar[1], 0u);
+        const unsigned arrived = atomicAdd(&bar[0], 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            atomicAdd(&bar[1], 1u);
+        } else {
+            unsigned it = 0;
+            while (atomicAdd(&bar[1], 0u) == gen) {
+                if (++it > (1u << 22)) {
+                    atomicExch(flag, 2);
+                    *stop_sh = 1;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
     }
     __syncthreads();
-    const int p = p_sh;
-    const double inv = (piv_sh != 0.0) ? 1.0 / piv_sh : 0.0;
-    for (int c = threadIdx.x; c < 2 * nb; c += blockDim.x) prow[c] = W[(int64_t)p * 2 * nb + c] * inv;
+    return *stop_sh == 0;
 }
 
-// eliminate column k from every row but the pivot row, which becomes prow
-__global__ void __launch_bounds__(256) k_gj_elim(double* __restrict__ W, int nb, int k, const int* __restrict__ perm,
-                                                 const double* __restrict__ prow) {
-    const int p = perm[k];
-    for (int r = blockIdx.x; r < nb; r += gridDim.x) {
-        double* row = W + (int64_t)r * 2 * nb;
-        if (r == p) {
-            for (int c = threadIdx.x; c < 2 * nb; c += blockDim.x) row[c] = prow[c];
-        } else {
-            const double f = row[k];
-            __syncthreads();
-            if (f != 0.0)
-                for (int c = threadIdx.x; c < 2 * nb; c += blockDim.x) row[c] -= f * prow[c];
+// Gauss-Jordan elimination with partial pivoting on W = [A | I] (row-major
+// nb x 2nb) in one cooperative launch: per column k every block finds the
+// same pivot (same data, same reduction order, own copy of the used-row
+// flags), eliminates column k from its rows (rows r = blockIdx.x mod
+// gridDim.x) with the unscaled pivot row, and meets the others at a grid
+// barrier.  Pivot rows are never scaled during the loop (no block writes the
+// row every block reads); the extraction divides by the pivots.  Global
+// reads of W go through L2 (ld.global.cg): other blocks wrote them.
+__global__ void __launch_bounds__(256) k_gj_coop(double* __restrict__ W, int nb, int* __restrict__ perm,
+                                                 int* __restrict__ flag, const double* __restrict__ tiny_p,
+                                                 unsigned* __restrict__ bar) {
+    extern __shared__ unsigned char used_sh[];
+    __shared__ double bv[8];
+    __shared__ int bi[8];
+    __shared__ int p_sh, stop_sh;
+    __shared__ double piv_sh;
+    const double tiny = tiny_p[0];
+    const int64_t ld = 2 * (int64_t)nb;
+    for (int r = threadIdx.x; r < nb; r += blockDim.x) used_sh[r] = 0;
+    if (threadIdx.x == 0) stop_sh = 0;
+    __syncthreads();
+    for (int k = 0; k < nb; k++) {
+        double best = -1.0;
+        int bidx = -1;
+        for (int r = threadIdx.x; r < nb; r += blockDim.x) {
+            if (used_sh[r]) continue;
+            const double a = fabs(__ldcg(W + r * ld + k));
+            if (a > best) { best = a; bidx = r; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+            if (ob > best || (ob == best && oi >= 0 && (bidx < 0 || oi < bidx))) { best = ob; bidx = oi; }
+        }
+        if ((threadIdx.x & 31) == 0) { bv[threadIdx.x >> 5] = best; bi[threadIdx.x >> 5] = bidx; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double b = -1.0;
+            int p = -1;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++)
+                if (bv[w] > b || (bv[w] == b && bi[w] >= 0 && (p < 0 || bi[w] < p))) { b = bv[w]; p = bi[w]; }
+            if (p < 0 || !(b > tiny)) {
+                if (blockIdx.x == 0) atomicExch(flag, 1);
+                p = (p < 0) ? 0 : p;
+            }
+            used_sh[p] = 1;
+            if (blockIdx.x == 0) perm[k] = p;
+            p_sh = p;
+            piv_sh = __ldcg(W + p * ld + k);
         }
         __syncthreads();
+        const int p = p_sh;
+        const double inv = (piv_sh != 0.0) ? 1.0 / piv_sh : 0.0;
+        const double* prow = W + p * ld;
+        for (int r = blockIdx.x; r < nb; r += gridDim.x) {
+            if (r == p) continue;
+            double* row = W + r * ld;
+            const double f = __ldcg(row + k);
+            if (f == 0.0) continue;
+            for (int64_t c = k + 1 + threadIdx.x; c < ld; c += blockDim.x) row[c] -= f * (__ldcg(prow + c) * inv);
+        }
+        // column k of the eliminated rows is zero; written once every thread
+        // of the block has read its multiplier f from it
+        __syncthreads();
+        for (int r = blockIdx.x + gridDim.x * threadIdx.x; r < nb; r += gridDim.x * blockDim.x)
+            if (r != p) W[r * ld + k] = 0.0;
+        if (!gj_grid_barrier(bar, gridDim.x, &stop_sh, flag)) break;
     }
 }
 
-// Ainv[k][j] = W[perm[k]][nb + j]
+// Ainv[k][j] = W[perm[k]][nb + j] / W[perm[k]][k] (the pivot rows were left
+// unscaled by the elimination)
 __global__ void k_gj_extract(const double* __restrict__ W, const int* __restrict__ perm, double* __restrict__ Ainv,
                              int nb) {
     const int64_t tot = (int64_t)nb * nb;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
         const int k = (int)(q / nb), j = (int)(q - (int64_t)k * nb);
-        Ainv[q] = W[(int64_t)perm[k] * 2 * nb + nb + j];
+        const double* row = W + (int64_t)perm[k] * 2 * nb;
+        Ainv[q] = row[nb + j] / row[k];
     }
 }
 
@@ -338,20 +383,30 @@ cudaError_t build_dense_inverse(int sym, const double* C, const double* diag, co
     double* E = work;                          // nb*nb
     double* Acol = work + (int64_t)nb * nb;    // nb*nb
     double* W = work + 2 * (int64_t)nb * nb;   // 2*nb*nb
-    double* prow = work + 4 * (int64_t)nb * nb;// 2*nb
     int* used = iwork;
     int* perm = iwork + nb;
+    unsigned* bar = reinterpret_cast<unsigned*>(work + 4 * (int64_t)nb * nb);  // 2 counters
     dim3 grd((unsigned)((G.N + 255) / 256), (unsigned)nb);
     if (sym == SYM_ISO) k_assemble<SYM_ISO><<<grd, 256, 0, s>>>(C, G, bc, E, Acol, nb);
     else k_assemble<SYM_MM><<<grd, 256, 0, s>>>(C, G, bc, E, Acol, nb);
     k_gj_init<<<152 * 4, 256, 0, s>>>(Acol, W, nb, used);
     k_pivot_threshold<<<1, 1024, 0, s>>>(diag, nb, 1e-12, tiny);
-    cudaMemsetAsync(flag, 0, sizeof(int), s);
-    const int eb = nb < 152 * 8 ? nb : 152 * 8;
-    for (int k = 0; k < nb; k++) {
-        k_gj_pivot<<<1, 1024, 0, s>>>(W, nb, k, used, perm, prow, flag, tiny);
-        k_gj_elim<<<eb, 256, 0, s>>>(W, nb, k, perm, prow);
-    }
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    // co-resident blocks for the grid barrier: at most one per SM, at most 64
+    int dev = 0, sms = 0, per_sm = 0, coop = 0;
+    const size_t smem = (size_t)nb;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_coop, 256, smem)) != cudaSuccess) return e;
+    if (!coop || per_sm < 1) return cudaErrorNotSupported;
+    int blocks = sms < 64 ? sms : 64;
+    if (blocks > nb) blocks = nb;
+    void* args[] = {&W, (void*)&nb, &perm, &flag, &tiny, &bar};
+    e = cudaLaunchCooperativeKernel((const void*)k_gj_coop, dim3(blocks), dim3(256), args, smem, s);
+    if (e != cudaSuccess) return e;
     k_gj_extract<<<152 * 4, 256, 0, s>>>(W, perm, Ainv, nb);
     return cudaGetLastError();
 }

@@ -91,7 +91,8 @@ typedef struct agb_solver_opts {
     int fine_kernel;          /* FP32 fine-level stencil kernels: 0 z-marching with TMA-staged stiffness
                                  (default), 1 one thread per node, 2 z-marching with register-staged stiffness */
     int krylov_reorth;        /* FGMRES Gram-Schmidt: 1 re-orthogonalise once, 0 single pass (default) */
-    int reserved_opts;
+    int tma_min_nodes;        /* FP32 levels with at least this many nodes use the z-marching kernels
+                                 (fine_kernel 0); smaller ones the per-node kernels (0: 30000) */
 } agb_solver_opts;
 
 typedef struct agb_solve_report {
