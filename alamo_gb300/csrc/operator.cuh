@@ -123,6 +123,19 @@ template <typename T, int SYM, typename UA, typename CF>
 __device__ __forceinline__ void boundary_rows(UA U, CF c, const LevelGeom<T>& G, const unsigned char* bt, int i,
                                               int j, int k, T f[3], T pa = T(1)) {
     T g[3][3], s[3][3], n[3];
+    const int cx = (i == 0) ? -1 : (i == G.nx - 1) ? 1 : 0;
+    const int cy = (j == 0) ? -1 : (j == G.ny - 1) ? 1 : 0;
+    const int cz = (k == 0) ? -1 : (k == G.nz - 1) ? 1 : 0;
+    const int reg = boundary_region<T>(cx, cy, cz, n);
+    const int t0 = bt[reg * 3], t1 = bt[reg * 3 + 1], t2 = bt[reg * 3 + 2];
+    // displacement (and periodic / none) rows read neither the gradient nor
+    // the stiffness: a region without traction or Neumann rows skips both
+    if (!(t0 == BC_TRAC || t0 == BC_NEUMANN || t1 == BC_TRAC || t1 == BC_NEUMANN || t2 == BC_TRAC ||
+          t2 == BC_NEUMANN)) {
+#pragma unroll
+        for (int r = 0; r < 3; r++) f[r] = bt[reg * 3 + r] == BC_DISP ? U(r, 0, 0, 0) : T(0);
+        return;
+    }
 #pragma unroll
     for (int p = 0; p < 3; p++) {
         const T u0 = U(p, 0, 0, 0);
@@ -130,16 +143,19 @@ __device__ __forceinline__ void boundary_rows(UA U, CF c, const LevelGeom<T>& G,
         g[p][1] = d1_of(j < G.ny - 1 ? U(p, 0, 1, 0) : u0, u0, j > 0 ? U(p, 0, -1, 0) : u0, j, G.ny, G.h[1], G.inv[1]);
         g[p][2] = d1_of(k < G.nz - 1 ? U(p, 0, 0, 1) : u0, u0, k > 0 ? U(p, 0, 0, -1) : u0, k, G.nz, G.h[2], G.inv[2]);
     }
-    stress_of<T, SYM>(c, g, s);
-    // sigma psi_avg (Elastic.cpp:195); pa = 1 without psi leaves s unchanged
+    if (t0 == BC_TRAC || t1 == BC_TRAC || t2 == BC_TRAC) {
+        stress_of<T, SYM>(c, g, s);
+        // sigma psi_avg (Elastic.cpp:195); pa = 1 without psi leaves s unchanged
 #pragma unroll
-    for (int p = 0; p < 3; p++)
+        for (int p = 0; p < 3; p++)
 #pragma unroll
-        for (int q = 0; q < 3; q++) s[p][q] *= pa;
-    const int cx = (i == 0) ? -1 : (i == G.nx - 1) ? 1 : 0;
-    const int cy = (j == 0) ? -1 : (j == G.ny - 1) ? 1 : 0;
-    const int cz = (k == 0) ? -1 : (k == G.nz - 1) ? 1 : 0;
-    const int reg = boundary_region<T>(cx, cy, cz, n);
+            for (int q = 0; q < 3; q++) s[p][q] *= pa;
+    } else {
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) s[p][q] = T(0);
+    }
 #pragma unroll
     for (int r = 0; r < 3; r++) f[r] = bc_component<T>(bt, reg, r, U(r, 0, 0, 0), g, s, n);
 }
