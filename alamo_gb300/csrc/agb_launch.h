@@ -70,7 +70,8 @@ cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStr
 cudaError_t launch_bc_init(double* b, const LevelGeom<double>& G, const BcTable& bc, const double* bcval_dev,
                            int homogeneous, cudaStream_t s);
 // Newton RHS (src/Solver/Nonlocal/Newton.H:144-231): dw = C (grad u - F0),
-// rhs = b - div dw (interior) or b - BC(u, grad u, dw) (boundary)
+// rhs = b - div dw (interior) or b - BC(u, grad u, dw) (boundary); u = nullptr
+// stands for u = 0 (nothing is read; without F0, rhs = b)
 cudaError_t launch_build_rhs(int sym, const double* u, const double* b, const double* F0, int f0_ncomp,
                              const double* C, const LevelGeom<double>& G, const BcTable& bc, double* dw, double* rhs,
                              cudaStream_t s);

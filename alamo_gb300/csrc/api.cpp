@@ -1323,7 +1323,7 @@ static agb_status build_rhs_dev(agb_elastic* h, const double* u, const double* b
     const int64_t N = nodes(h);
     if (!h->dw) CK(cudaMalloc(&h->dw, sizeof(double) * 9 * N));
     CK(launch_build_rhs(h->sym, u, b, F0, f0n, h->L64[0].C, h->L64[0].G, h->bc, h->dw, rhs, h->stream));
-    h->launches += 2;
+    h->launches += (u || f0n) ? 2 : 0;  // u = 0 without F0: a device copy
     return AGB_OK;
 }
 
@@ -1439,8 +1439,7 @@ agb_status agb_elastic_learned_guess(agb_elastic* h, agb_unet* net, const double
     TRY(ensure_io(h, 2, 2 * bytes));
     double* rhs0 = h->io[2];
     double* rg = h->io[2] + 3 * N;
-    CK(cudaMemsetAsync(rg, 0, bytes, h->stream));
-    TRY(build_rhs_dev(h, rg, (const double*)db, (const double*)dF, f0_ncomp, rhs0));
+    TRY(build_rhs_dev(h, nullptr, (const double*)db, (const double*)dF, f0_ncomp, rhs0));
     // fallback test: rhs0 - A x at the guess against rhs0 (x = 0), both
     // restricted to the network's level -- the smooth part of the residual,
     // which the cycles reduce slowly and a coarse guess can reduce; the

@@ -348,37 +348,42 @@ cudaError_t launch_restrict_C(const double* Cf, const LevelGeom<double>& Gf, dou
 template <typename T>
 __global__ void __launch_bounds__(256) k_prolong_add(const T* __restrict__ crse, LevelGeom<T> Gc, T* __restrict__ fine,
                                                      LevelGeom<T> G) {
-    AGB_NODE_INDEX
-    if (!live) return;
-    const int I = i >> 1, J = j >> 1, K = k >> 1;
-    const int oi = i & 1, oj = j & 1, ok = k & 1;
-    const int64_t cid = I + Gc.sy * J + Gc.sz * K;
-    const int64_t dx = oi, dy = oj ? Gc.sy : 0, dz = ok ? Gc.sz : 0;
+    // one thread per coarse column I and fine row (j, k): fine nodes 2I
+    // (weight 1 at I) and 2I+1 (1/2 at I and I+1) along x; the (j, k) parity
+    // picks the coarse rows averaged first, uniform across a warp.  R(I+1)
+    // comes from the next lane (the warp's last lane reads it).
+    const int I = blockIdx.x * BX + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    const int k = blockIdx.z * BZ + threadIdx.z;
+    const bool live = (I < Gc.nx) & (j < G.ny) & (k < G.nz);
+    const int J = j >> 1, K = k >> 1, oj = j & 1, ok = k & 1;
+    const int64_t dy = oj ? Gc.sy : 0, dz = ok ? Gc.sz : 0;
+    auto rowavg = [&](const T* cc) -> T {
+        if (oj & ok) return T(0.25) * ((cc[0] + cc[dy]) + (cc[dz] + cc[dy + dz]));
+        if (oj | ok) return T(0.5) * (cc[0] + cc[dy + dz]);
+        return cc[0];
+    };
+    const int64_t cid = (int64_t)I + Gc.sy * J + Gc.sz * K;
+    const int64_t fid = 2 * (int64_t)I + G.sy * j + G.sz * (int64_t)k;
+    const bool odd = live && (I + 1 < Gc.nx);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         const T* cc = crse + c * Gc.N + cid;
-        T v;
-        const int odd = oi + oj + ok;
-        if (odd == 0) v = cc[0];
-        else if (odd == 1) v = T(0.5) * (cc[0] + cc[dx + dy + dz]);
-        else if (odd == 2) {
-            // face centre: the two odd directions span the four corners
-            int64_t a, b2;
-            if (!oi) { a = dy; b2 = dz; }
-            else if (!oj) { a = dx; b2 = dz; }
-            else { a = dx; b2 = dy; }
-            v = T(0.25) * (cc[0] + cc[a] + cc[b2] + cc[a + b2]);
-        } else {
-            v = T(0.125) * (cc[0] + cc[dx] + cc[dy] + cc[dz] + cc[dy + dz] + cc[dx + dz] + cc[dx + dy] + cc[dx + dy + dz]);
+        const T R = live ? rowavg(cc) : T(0);
+        T Rn = __shfl_down_sync(0xffffffffu, R, 1);
+        if (threadIdx.x == BX - 1 && odd) Rn = rowavg(cc + 1);
+        if (live) {
+            T* f = fine + c * G.N + fid;
+            f[0] += R;
+            if (odd) f[1] += T(0.5) * (R + Rn);
         }
-        fine[c * G.N + id] += v;
     }
 }
 
 template <typename T>
 cudaError_t launch_prolong_add(const T* crse, const LevelGeom<T>& Gc, T* fine, const LevelGeom<T>& Gf,
                                cudaStream_t s) {
-    dim3 blk(BX, BY, BZ), grd = grid3(Gf.nx, Gf.ny, Gf.nz);
+    dim3 blk(BX, BY, BZ), grd = grid3(Gc.nx, Gf.ny, Gf.nz);
     k_prolong_add<T><<<grd, blk, 0, s>>>(crse, Gc, fine, Gf);
     return cudaGetLastError();
 }
@@ -522,15 +527,23 @@ __device__ __forceinline__ double f0_at(const double* F0, int f0n, int64_t id, i
     return 0.0;
 }
 
-// dw = C (grad u - F0), stored SoA as 9 components (row-major p*3+q)
-template <int SYM>
+// dw = C (grad u - F0), stored SoA as 9 components (row-major p*3+q);
+// ZERO_U: u = 0 (the Newton step from zero), no displacement is read
+template <int SYM, bool ZERO_U>
 __global__ void __launch_bounds__(256) k_dw(const double* __restrict__ u, const double* __restrict__ F0, int f0n,
                                             const double* __restrict__ C, LevelGeom<double> G,
                                             double* __restrict__ dw) {
     AGB_NODE_INDEX
     if (!live) return;
     double g[3][3], s[3][3];
-    grad_at(u, G, i, j, k, id, g);
+    if (ZERO_U) {
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) g[p][q] = 0.0;
+    } else {
+        grad_at(u, G, i, j, k, id, g);
+    }
 #pragma unroll
     for (int p = 0; p < 3; p++)
 #pragma unroll
@@ -544,6 +557,7 @@ __global__ void __launch_bounds__(256) k_dw(const double* __restrict__ u, const 
         for (int q = 0; q < 3; q++) dw[(p * 3 + q) * N + id] = s[p][q];
 }
 
+template <bool ZERO_U>
 __global__ void __launch_bounds__(256) k_rhs(const double* __restrict__ u, const double* __restrict__ b,
                                              const double* __restrict__ dw, LevelGeom<double> G, BcTable bc,
                                              double* __restrict__ rhs) {
@@ -556,14 +570,21 @@ __global__ void __launch_bounds__(256) k_rhs(const double* __restrict__ u, const
     double ret[3];
     if (cx | cy | cz) {
         double g[3][3], s[3][3], n[3];
-        grad_at(u, G, i, j, k, id, g);
+        if (ZERO_U) {
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int q = 0; q < 3; q++) g[p][q] = 0.0;
+        } else {
+            grad_at(u, G, i, j, k, id, g);
+        }
 #pragma unroll
         for (int p = 0; p < 3; p++)
 #pragma unroll
             for (int q = 0; q < 3; q++) s[p][q] = dw[(p * 3 + q) * N + id];
         const int reg = boundary_region<double>(cx, cy, cz, n);
 #pragma unroll
-        for (int r = 0; r < 3; r++) ret[r] = bc_component<double>(bc.t, reg, r, u[r * N + id], g, s, n);
+        for (int r = 0; r < 3; r++) ret[r] = bc_component<double>(bc.t, reg, r, ZERO_U ? 0.0 : u[r * N + id], g, s, n);
     } else {
         // div dw with central differences (src/Numeric/Stencil.H:588-657)
         const int64_t off[3] = {1, G.sy, G.sz};
@@ -595,11 +616,23 @@ cudaError_t launch_build_rhs(int sym, const double* u, const double* b, const do
                              const double* C, const LevelGeom<double>& G, const BcTable& bc, double* dw, double* rhs,
                              cudaStream_t s) {
     dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
-    if (sym == SYM_ISO) k_dw<SYM_ISO><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
-    else k_dw<SYM_MM><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
+    if (u == nullptr && f0_ncomp == 0) {
+        // u = 0 and no eigenstrain: dw = 0, every row of b - (BC rows / div dw)
+        // subtracts an exact zero, so rhs = b
+        if (rhs == b) return cudaSuccess;
+        return cudaMemcpyAsync(rhs, b, sizeof(double) * 3 * G.N, cudaMemcpyDeviceToDevice, s);
+    }
+    if (u == nullptr) {
+        if (sym == SYM_ISO) k_dw<SYM_ISO, true><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
+        else k_dw<SYM_MM, true><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
+    } else {
+        if (sym == SYM_ISO) k_dw<SYM_ISO, false><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
+        else k_dw<SYM_MM, false><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_rhs<<<grd, blk, 0, s>>>(u, b, dw, G, bc, rhs);
+    if (u == nullptr) k_rhs<true><<<grd, blk, 0, s>>>(u, b, dw, G, bc, rhs);
+    else k_rhs<false><<<grd, blk, 0, s>>>(u, b, dw, G, bc, rhs);
     return cudaGetLastError();
 }
 

@@ -217,3 +217,22 @@ def test_learned_guess_transfers_and_fallback(agb, oracle):
         u0 = np.zeros((3, n, n, n))
         agb.Newton(op).solve(u0, b, F0, tol_rel=1e-10, tol_abs=0.0)
         assert np.abs(x - u0).max() <= 1e-5 * np.abs(u0).max()
+
+
+@pytest.mark.gpu
+def test_learned_guess_rhs_without_eigenstrain(agb, oracle):
+    """Without F0 the Newton right-hand side at zero displacement is b
+    itself (every subtracted row is an exact zero); the guess path takes
+    that shortcut and must agree with the oracle's full RHS bit for bit."""
+    from alamo_gb300 import learn
+    n = 33
+    C, F0, bc, dx = P.voronoi_clamp(n)
+    with learn.UNet(17, seed=6) as net, agb.Elastic(n, dx, "majorminor") as op:
+        op.SetModel(np.ascontiguousarray(C))
+        op.SetBC(bc)
+        b = op.bc_init()
+        u, rhs, _, used = learn.learned_guess(op, net, b, None)
+    bt, _ = bc.tables()
+    ref = oracle.build_rhs(C, None, bt, np.zeros((3, n, n, n)), b, dx)
+    assert np.array_equal(rhs, ref)
+    assert np.array_equal(rhs, b)
