@@ -42,6 +42,8 @@ cudaError_t launch_restrict(const T* fine, const LevelGeom<T>& Gf, T* crse, cons
 // same weights on nc stiffness components (SoA)
 cudaError_t launch_restrict_C(const double* Cf, const LevelGeom<double>& Gf, double* Cc, const LevelGeom<double>& Gc,
                               int nc, cudaStream_t s);
+cudaError_t launch_restrict_C(const float* Cf, const LevelGeom<float>& Gf, float* Cc, const LevelGeom<float>& Gc,
+                              int nc, cudaStream_t s);
 // fine += P crse (trilinear nodal prolongation)
 template <typename T>
 cudaError_t launch_prolong_add(const T* crse, const LevelGeom<T>& Gc, T* fine, const LevelGeom<T>& Gf,

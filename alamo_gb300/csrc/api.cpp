@@ -135,6 +135,9 @@ struct agb_elastic {
     Krylov<float> K32;
     // dense direct bottom solve
     double* bot_inv = nullptr;
+    // which coarsest operator the inverse was built from: 0 none (stale),
+    // 64 the FP64 hierarchy, 32 the FP32 hierarchy widened to FP64
+    int bot_src = 0;
     int bot_nb = 0;
     bool bot_dense = false;
     // buffers of its build (assembly + one cooperative Gauss-Jordan launch)
@@ -330,12 +333,21 @@ static constexpr int64_t TMA_MIN_NODES = 30000;  // default of agb_solver_opts::
 
 // FP32 copies of every level's stiffness and diagonal; for the levels the
 // TMA stencil kernels sweep also the padded copy and its tensor map
+// FP32 hierarchy.  With the FP64 hierarchy built (h->prepared) every level
+// is its FP64 stiffness rounded; otherwise (the mixed-precision solve on its
+// own) level 0 is rounded and the coarser levels are coarsened in FP32 --
+// the preconditioner's coarse operators then differ from the FP64 ones by
+// FP32 rounding, and the FP64 hierarchy, whose coarsening is FP64-pipe
+// bound, is built only when an FP64 operation needs it.
 agb_status build_f32(agb_elastic* h) {
     const int nl = (int)h->L64.size();
     if (h->L32.size() != h->L64.size()) TRY(alloc_levels32(h));
     for (int l = 0; l < nl; l++) {
         Lev<float>& v = h->L32[l];
-        CK(launch_to_float(h->L64[l].C, v.C, h->L64[l].G.N * h->nc, 1.0, h->stream));
+        if (h->prepared || l == 0)
+            CK(launch_to_float(h->L64[l].C, v.C, h->L64[l].G.N * h->nc, 1.0, h->stream));
+        else
+            CK(launch_restrict_C(h->L32[l - 1].C, h->L32[l - 1].G, v.C, v.G, h->nc, h->stream));
         h->launches++;
         if (h->psi_set) {
             const int64_t np = v.G.psz * (v.G.nz + 1);
@@ -380,16 +392,10 @@ agb_status build_f32(agb_elastic* h) {
     return AGB_OK;
 }
 
-agb_status prepare(agb_elastic* h) {
-    if (h->prepared) return AGB_OK;
-    if (!h->model_set) return fail(AGB_NOT_READY, "model not set (agb_elastic_set_model)");
+// psi on every level (Elastic::averageDownCoeffsSameAmrLevel,
+// src/Operator/Elastic.cpp:839-905), before the diagonals that use it
+agb_status prepare_psi(agb_elastic* h) {
     const int nl = (int)h->L64.size();
-    for (int l = 1; l < nl; l++) {
-        CK(launch_restrict_C(h->L64[l - 1].C, h->L64[l - 1].G, h->L64[l].C, h->L64[l].G, h->nc, h->stream));
-        h->launches++;
-    }
-    // psi on every level (Elastic::averageDownCoeffsSameAmrLevel,
-    // src/Operator/Elastic.cpp:839-905), before the diagonal that uses it
     for (int l = 0; l < nl; l++) {
         Lev<double>& v = h->L64[l];
         if (!h->psi_set) {
@@ -406,22 +412,60 @@ agb_status prepare(agb_elastic* h) {
         }
         v.G.psi_small = h->psi_small;
     }
+    return AGB_OK;
+}
+
+// Operator<Grid::Node>::prepareForSolve (src/Operator/Operator.cpp:253-260)
+// in FP64: stiffness and psi on every level, every level's diagonal, and the
+// direct bottom's inverse from the FP64 coarsest operator
+agb_status prepare(agb_elastic* h) {
+    if (h->prepared) return AGB_OK;
+    if (!h->model_set) return fail(AGB_NOT_READY, "model not set (agb_elastic_set_model)");
+    const int nl = (int)h->L64.size();
+    for (int l = 1; l < nl; l++) {
+        CK(launch_restrict_C(h->L64[l - 1].C, h->L64[l - 1].G, h->L64[l].C, h->L64[l].G, h->nc, h->stream));
+        h->launches++;
+    }
+    TRY(prepare_psi(h));
     for (int l = 0; l < nl; l++) {
         CK(launch_diagonal<double>(h->sym, h->L64[l].C, h->L64[l].G, h->bc, h->L64[l].diag, h->stream));
         h->launches++;
     }
-    h->bot_dense = false;
-    if (h->opts.bottom_solver == AGB_BOTTOM_DIRECT) TRY(build_bottom_dense(h));
-    if (h->opts.precision == AGB_PRECISION_MIXED) TRY(build_f32(h));
+    if (h->opts.bottom_solver != AGB_BOTTOM_DIRECT) {
+        h->bot_dense = false;
+    } else if (h->bot_src != 64) {
+        h->bot_dense = false;
+        TRY(build_bottom_dense(h));
+        h->bot_src = 64;
+    }
     CK(cudaStreamSynchronize(h->stream));
     h->prepared = true;
     return AGB_OK;
 }
 
+// The FP32 hierarchy of the mixed-precision cycles.  Without the FP64
+// hierarchy, the FP64 coarsest level (the bottom solve's, which stays FP64)
+// is the FP32 one widened, with its FP64 diagonal.
 agb_status ensure_f32(agb_elastic* h) {
-    TRY(prepare(h));
     if (h->have_f32) return AGB_OK;
+    if (!h->model_set) return fail(AGB_NOT_READY, "model not set (agb_elastic_set_model)");
+    if (!h->prepared) TRY(prepare_psi(h));
     TRY(build_f32(h));
+    if (!h->prepared) {
+        Lev<double>& d = h->L64.back();
+        const Lev<float>& f = h->L32.back();
+        CK(cudaMemsetAsync(d.C, 0, sizeof(double) * d.G.N * h->nc, h->stream));
+        CK(launch_add_float(f.C, d.C, d.G.N * h->nc, 1.0, h->stream));
+        CK(launch_diagonal<double>(h->sym, d.C, d.G, h->bc, d.diag, h->stream));
+        h->launches += 2;
+        if (h->opts.bottom_solver != AGB_BOTTOM_DIRECT) {
+            h->bot_dense = false;
+        } else if (h->bot_src == 0) {
+            h->bot_dense = false;
+            TRY(build_bottom_dense(h));
+            h->bot_src = 32;
+        }
+    }
     CK(cudaStreamSynchronize(h->stream));
     return AGB_OK;
 }
@@ -744,9 +788,11 @@ agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, doub
 agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_rel, double tol_abs,
                      agb_solve_report* rep, bool x_zero = false) {
     auto t0 = std::chrono::steady_clock::now();
-    TRY(prepare(h));
     const bool mixed = h->opts.precision == AGB_PRECISION_MIXED;
+    // the mixed solve needs the FP32 hierarchy and the fine FP64 stiffness
+    // only; the FP64 one needs the FP64 hierarchy
     if (mixed) TRY(ensure_f32(h));
+    else TRY(prepare(h));
     Lev<double>& top = h->L64[0];
     const int64_t n3 = 3 * top.G.N;
     double r[2], bn[2];
@@ -1032,6 +1078,7 @@ agb_status agb_elastic_set_opts(agb_elastic* h, const agb_solver_opts* o) {
     }
     h->prepared = false;
     h->have_f32 = false;
+    h->bot_src = 0;
     return AGB_OK;
 }
 
@@ -1065,6 +1112,7 @@ agb_status agb_elastic_set_model(agb_elastic* h, const double* C, int where) {
     h->model_set = true;
     h->prepared = false;
     h->have_f32 = false;
+    h->bot_src = 0;
     return AGB_OK;
 }
 
@@ -1089,6 +1137,7 @@ agb_status agb_elastic_set_bc(agb_elastic* h, const int* type, const double* val
     h->bc_set = true;
     h->prepared = false;
     h->have_f32 = false;
+    h->bot_src = 0;
     return AGB_OK;
 }
 
@@ -1128,6 +1177,7 @@ agb_status agb_elastic_set_psi(agb_elastic* h, const double* psi, double small, 
     }
     h->prepared = false;
     h->have_f32 = false;
+    h->bot_src = 0;
     return AGB_OK;
 }
 

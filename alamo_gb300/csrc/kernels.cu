@@ -324,22 +324,29 @@ template cudaError_t launch_restrict<float>(const float*, const LevelGeom<float>
                                             cudaStream_t);
 
 // C coarsening (src/Operator/Elastic.cpp:786-834): same weights per entry
-__global__ void __launch_bounds__(256) k_restrict_C(const double* __restrict__ Cf, LevelGeom<double> Gf,
-                                                    double* __restrict__ Cc, LevelGeom<double> G, int nc) {
+template <typename T>
+__global__ void __launch_bounds__(256) k_restrict_C(const T* __restrict__ Cf, LevelGeom<T> Gf, T* __restrict__ Cc,
+                                                    LevelGeom<T> G, int nc) {
     AGB_NODE_INDEX
     if (!live) return;
     const int64_t fid = 2 * i + Gf.sy * (2 * j) + Gf.sz * (2 * k);
     for (int c = 0; c < nc; c++) {
-        const double* fc = Cf + c * Gf.N + fid;
+        const T* fc = Cf + c * Gf.N + fid;
         auto f = [&](int a, int b, int d) { return fc[a + Gf.sy * b + Gf.sz * d]; };
-        Cc[c * G.N + id] = restrict_point<double>(f, i, j, k, G.nx, G.ny, G.nz);
+        Cc[c * G.N + id] = restrict_point<T>(f, i, j, k, G.nx, G.ny, G.nz);
     }
 }
 
 cudaError_t launch_restrict_C(const double* Cf, const LevelGeom<double>& Gf, double* Cc, const LevelGeom<double>& Gc,
                               int nc, cudaStream_t s) {
     dim3 blk(BX, BY, BZ), grd = grid3(Gc.nx, Gc.ny, Gc.nz);
-    k_restrict_C<<<grd, blk, 0, s>>>(Cf, Gf, Cc, Gc, nc);
+    k_restrict_C<double><<<grd, blk, 0, s>>>(Cf, Gf, Cc, Gc, nc);
+    return cudaGetLastError();
+}
+cudaError_t launch_restrict_C(const float* Cf, const LevelGeom<float>& Gf, float* Cc, const LevelGeom<float>& Gc,
+                              int nc, cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(Gc.nx, Gc.ny, Gc.nz);
+    k_restrict_C<float><<<grd, blk, 0, s>>>(Cf, Gf, Cc, Gc, nc);
     return cudaGetLastError();
 }
 
