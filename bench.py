@@ -11,8 +11,8 @@ bottom-level inverse), the learned initial guess (U-Net on the 65^3 level,
 with its residual-based fallback to zero; --guess '' skips it), the Newton
 right-hand side and the solve to 1e-8 relative residual (inf-norm of the
 FP64 residual, tol_abs = 0).  Fast path: FGMRES preconditioned by one
-V-cycle, both in FP32, inside FP64 iterative refinement, with a direct solve
-on a 5^3-node bottom level.  The plain FP64 comparison is the reference's
+V(1,1)-cycle, both in FP32, inside FP64 iterative refinement, with a direct
+solve on a 5^3-node bottom level.  The plain FP64 comparison is the reference's
 algorithm on the GPU: V(2,2) cycles with damped Jacobi and the BiCGStab
 bottom, everything FP64, from zero.  `value` is seconds per solve (lower is
 better); `e2e` is the same solve through the C ABI with host buffers
@@ -51,11 +51,13 @@ BYTES_PER_NODE = {
 }
 FAMILY = {"fapply_f64": 0, "jacobi_f64": 1, "residual_f64": 2, "fapply_f32": 3, "jacobi_f32": 4, "residual_f32": 5,
           "restrict": 6, "prolong": 7, "bottom": 8}
-# dram__bytes_read.sum + dram__bytes_write.sum per node of the fine-level
-# interior sweep, from the 129^3 capture summarised in
-# profiles/k_zmarch_tma_jacobi_mm_129.md (283.9 MB + 19.3 MB over 2,146,689
-# nodes); the sweep streams every array once, so it scales with the nodes
-TRAFFIC_PER_NODE = {("jacobi_f32", 21): (283.893248e6 + 19.328e6) / 2146689}
+# dram__bytes_read.sum + dram__bytes_write.sum of one fine-level Jacobi
+# sweep from 129^3 captures: the interior sweep per node (283.9 MB + 19.3 MB
+# over 2,146,689 nodes, profiles/k_zmarch_tma_jacobi_mm_129.md; it streams
+# every array once, so it scales with the nodes) and the boundary-face
+# kernel per boundary node (28.1 MB + 0.1 MB over 98,306 boundary nodes,
+# profiles/k_zt_faces_mm_129.md); (per node, per boundary node)
+TRAFFIC_PER_NODE = {("jacobi_f32", 21): ((283.893248e6 + 19.328e6) / 2146689, (28.08704e6 + 0.097536e6) / 98306)}
 
 
 def parse():
@@ -342,8 +344,9 @@ def main():
         alg_bytes = BYTES_PER_NODE[dom][nc] * N
         achieved = alg_bytes / per_launch_s / 1e9
         traf = TRAFFIC_PER_NODE.get((dom, nc))
+        nb = N - (n - 2) ** 3  # boundary nodes
         roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": traf * N if traf else None,
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traf[0] * N + traf[1] * nb if traf else None,
                 "peak_source": peak_kind, "launches": cnt, "avg_launch_ms": ms / cnt,
                 "alg_bytes_per_launch": alg_bytes, "share_of_step": ms / 1e3 / (sec * args.steps)}
     kernels = {k: {"launches": v[0], "ms": v[1]} for k, v in fam.items() if v[0] > 0}
