@@ -1095,12 +1095,12 @@ agb_status agb_elastic_set_model(agb_elastic* h, const double* C, int where) {
     const size_t bytes = sizeof(double) * N * h->nc;
     const void* src = nullptr;
     if (where == AGB_MEM_HOST) {
-        // stage through a stream-ordered temporary, then AoS -> SoA
-        double* tmp = nullptr;
-        CK(cudaMallocAsync((void**)&tmp, bytes, h->stream));
+        // stage through the handle's persistent staging buffer (no
+        // allocation per call), then AoS -> SoA
+        TRY(ensure_io(h, 0, bytes));
+        double* tmp = h->io[0];
         CK(cudaMemcpyAsync(tmp, C, bytes, cudaMemcpyHostToDevice, h->stream));
         CK(launch_aos_to_soa(tmp, h->L64[0].C, N, h->nc, h->stream));
-        CK(cudaFreeAsync(tmp, h->stream));
     } else if (where == AGB_MEM_DEVICE) {
         src = C;
         CK(launch_aos_to_soa((const double*)src, h->L64[0].C, N, h->nc, h->stream));
@@ -1454,12 +1454,11 @@ agb_status agb_newton_solve(agb_elastic* h, double* u, const double* b, const do
     return agb_newton_solve_n(h, u, b, F0, f0_ncomp, tol_rel, tol_abs, 1, 0.0, rep, nullptr, where);
 }
 
-agb_status agb_elastic_learned_guess(agb_elastic* h, agb_unet* net, const double* b, const double* F0, int f0_ncomp,
-                                     double* u, double* rhs, double norms[2], int* used, int where) {
-    if (!h || !net || !b || !u) return fail(AGB_BAD_ARG, "null argument");
-    if (!(f0_ncomp == 0 || f0_ncomp == 1 || f0_ncomp == 9) || (f0_ncomp && !F0))
-        return fail(AGB_BAD_ARG, "f0_ncomp must be 0, 1 or 9 (with F0 given)");
-    if (!h->model_set) return fail(AGB_NOT_READY, "model not set");
+// The learned guess on device data: the guess ends in the fine level's cor
+// buffer (zero when the fallback fires), the Newton right-hand side at zero
+// in io[2] (first 3N doubles); io[2] is scratch, slots 1 and 3 untouched.
+static agb_status learned_guess_dev(agb_elastic* h, agb_unet* net, const void* db, const void* dF, int f0_ncomp,
+                                    double norms[2], int* used, double** rhs_out) {
     const int ng = unet_grid(net);
     int lg = -1;
     for (int l = 0; l < (int)h->L64.size(); l++) {
@@ -1469,9 +1468,6 @@ agb_status agb_elastic_learned_guess(agb_elastic* h, agb_unet* net, const double
     if (lg < 0) return fail(AGB_BAD_ARG, "no multigrid level of the handle has the network's grid");
     const int64_t N = nodes(h);
     const size_t bytes = sizeof(double) * 3 * N;
-    const void *db = nullptr, *dF = nullptr;
-    TRY(dev_in(h, 1, b, bytes, where, &db));
-    if (f0_ncomp) TRY(dev_in(h, 3, F0, sizeof(double) * f0_ncomp * N, where, &dF));
     // features on the fine level, restricted to the network's level (the
     // levels' rescor buffers are free outside a solve); prediction in cor
     std::vector<Lev<double>>& L = h->L64;
@@ -1533,11 +1529,58 @@ agb_status agb_elastic_learned_guess(agb_elastic* h, agb_unet* net, const double
     if (norms) { norms[0] = ng_[1]; norms[1] = nz_[1]; }
     if (used) *used = ok ? 1 : 0;
     if (!ok) CK(cudaMemsetAsync(L[0].cor, 0, bytes, h->stream));
+    *rhs_out = rhs0;
+    return AGB_OK;
+}
+
+static agb_status check_guess_args(agb_elastic* h, agb_unet* net, const double* b, const double* u, const double* F0,
+                                   int f0_ncomp) {
+    if (!h || !net || !b || !u) return fail(AGB_BAD_ARG, "null argument");
+    if (!(f0_ncomp == 0 || f0_ncomp == 1 || f0_ncomp == 9) || (f0_ncomp && !F0))
+        return fail(AGB_BAD_ARG, "f0_ncomp must be 0, 1 or 9 (with F0 given)");
+    if (!h->model_set) return fail(AGB_NOT_READY, "model not set");
+    return AGB_OK;
+}
+
+agb_status agb_elastic_learned_guess(agb_elastic* h, agb_unet* net, const double* b, const double* F0, int f0_ncomp,
+                                     double* u, double* rhs, double norms[2], int* used, int where) {
+    TRY(check_guess_args(h, net, b, u, F0, f0_ncomp));
+    const int64_t N = nodes(h);
+    const size_t bytes = sizeof(double) * 3 * N;
+    const void *db = nullptr, *dF = nullptr;
+    TRY(dev_in(h, 1, b, bytes, where, &db));
+    if (f0_ncomp) TRY(dev_in(h, 3, F0, sizeof(double) * f0_ncomp * N, where, &dF));
+    double* rhs0 = nullptr;
+    TRY(learned_guess_dev(h, net, db, dF, f0_ncomp, norms, used, &rhs0));
     const cudaMemcpyKind kind = where == AGB_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    CK(cudaMemcpyAsync(u, L[0].cor, bytes, kind, h->stream));
+    CK(cudaMemcpyAsync(u, h->L64[0].cor, bytes, kind, h->stream));
     if (rhs) CK(cudaMemcpyAsync(rhs, rhs0, bytes, kind, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return AGB_OK;
+}
+
+agb_status agb_newton_solve_guess(agb_elastic* h, agb_unet* net, double* u, const double* b, const double* F0,
+                                  int f0_ncomp, double tol_rel, double tol_abs, agb_solve_report* rep, int* used,
+                                  int where) {
+    TRY(check_guess_args(h, net, b, u, F0, f0_ncomp));
+    auto t0 = std::chrono::steady_clock::now();
+    const int64_t N = nodes(h);
+    const size_t bytes = sizeof(double) * 3 * N;
+    const void *db = nullptr, *dF = nullptr;
+    void* du = nullptr;
+    TRY(dev_in(h, 1, b, bytes, where, &db));
+    if (f0_ncomp) TRY(dev_in(h, 3, F0, sizeof(double) * f0_ncomp * N, where, &dF));
+    TRY(dev_out(h, 0, u, bytes, where, &du));
+    double* rhs0 = nullptr;
+    int ok = 0;
+    TRY(learned_guess_dev(h, net, db, dF, f0_ncomp, nullptr, &ok, &rhs0));
+    if (used) *used = ok;
+    CK(cudaMemcpyAsync(du, h->L64[0].cor, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    const agb_status st = solve_dev(h, (double*)du, rhs0, tol_rel, tol_abs, rep, ok == 0);
+    if (st != AGB_OK && st != AGB_NOT_CONVERGED) return st;
+    TRY(finish_out(h, u, du, bytes, where));
+    if (rep) rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return st;
 }
 
 agb_status agb_elastic_stress_strain(agb_elastic* h, const double* u, const double* F0, int f0_ncomp, double* stress,

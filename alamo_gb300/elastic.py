@@ -365,3 +365,20 @@ class Newton(Linear):
         if rn is not None:
             d["relnorm"] = rn
         return d
+
+    def solve_guess(self, net, u, b, F0=None, tol_rel=1e-8, tol_abs=0.0, allow_not_converged=False):
+        """One Newton step from u = 0 whose linear solve starts from the
+        learned guess of `net` (agb_newton_solve_guess): u is output only.
+        Returns the solve report as a dict plus "guess_used"."""
+        rep = L.SolveReport()
+        pF, nF, wF = Elastic._f0(F0)
+        pu, wu = _arg(u)
+        pb, wb = _arg(b)
+        used = ctypes.c_int()
+        st = L.lib().agb_newton_solve_guess(self.op.h, net.h, pu, pb, pF, nF, ctypes.c_double(tol_rel),
+                                            ctypes.c_double(tol_abs), ctypes.byref(rep), ctypes.byref(used),
+                                            _same_where(wu, wb, wF))
+        L.check(st, (L.AGB_OK, L.AGB_NOT_CONVERGED) if allow_not_converged else (L.AGB_OK,))
+        d = rep.as_dict()
+        d["guess_used"] = bool(used.value)
+        return d

@@ -359,14 +359,12 @@ def main():
         u_h = torch.zeros_like(b_h).pin_memory()
         F0_h = torch.from_numpy(F0).pin_memory() if F0 is not None else None
 
-        rhs_h = torch.zeros_like(b_h).pin_memory()
 
         def step_host():
             op.SetModel(C_h.numpy())
             F0x = F0_h.numpy() if F0_h is not None else None
             if net is not None:
-                learn.learned_guess(op, net, b_h.numpy(), F0x, u_h.numpy(), rhs_h.numpy())
-                linear.solve(u_h.numpy(), rhs_h.numpy(), 1e-8, 0.0)
+                newton.solve_guess(net, u_h.numpy(), b_h.numpy(), F0x, tol_rel=1e-8, tol_abs=0.0)
             else:
                 u_h.zero_()
                 newton.solve(u_h.numpy(), b_h.numpy(), F0x, tol_rel=1e-8, tol_abs=0.0)
@@ -384,13 +382,10 @@ def main():
         if dist is not None:
             dist.all_reduce(te, op=dist.ReduceOp.MAX)
         vec = 3 * N * 8
-        if net is not None:
-            # guess: b, F0 in; guess and right-hand side out; solve: both in, u out
-            h2d = C.nbytes + 3 * vec + (F0.nbytes if F0 is not None else 0)
-            d2h = 3 * vec
-        else:
-            h2d = C.nbytes + 2 * vec + (F0.nbytes if F0 is not None else 0)
-            d2h = vec
+        # stiffness, b (and F0) in, u out; the guess path's u is output only,
+        # the plain Newton step copies its zero u in
+        h2d = C.nbytes + (vec if net is not None else 2 * vec) + (F0.nbytes if F0 is not None else 0)
+        d2h = vec
         e2e = {"value": float(te.item()), "unit": "s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "timing": "host wall clock around synchronous C-ABI calls"}
 

@@ -282,6 +282,15 @@ agb_status agb_unet_predict(agb_unet* net, const double* features, double* u, in
  * guess, norms[1] = at zero. */
 agb_status agb_elastic_learned_guess(agb_elastic* h, agb_unet* net, const double* b, const double* F0, int f0_ncomp,
                                      double* u, double* rhs, double norms[2], int* used, int where);
+/* Newton::solve (src/Solver/Nonlocal/Newton.H:279-358, nriters = 1, u = 0 on
+ * entry) with the learned guess as the first iterate of the step's linear
+ * solve, in one call: agb_elastic_learned_guess then agb_linear_solve on
+ * device data, so host callers copy b (and F0) in and u out once.  u is
+ * output only (the step starts from zero); used (may be NULL) reports
+ * whether the guess was kept. */
+agb_status agb_newton_solve_guess(agb_elastic* h, agb_unet* net, double* u, const double* b, const double* F0,
+                                  int f0_ncomp, double tol_rel, double tol_abs, agb_solve_report* rep, int* used,
+                                  int where);
 /* Test hook of the tensor-core convolution: X [V][Cin] BF16 channels-last
  * (device), W [Cout][Cin][27] FP32, bias [Cout] FP32 (may be NULL), output
  * Y (BF16) or Yf (FP32), exactly one non-NULL; stream may be NULL. */

@@ -236,3 +236,35 @@ def test_learned_guess_rhs_without_eigenstrain(agb, oracle):
     ref = oracle.build_rhs(C, None, bt, np.zeros((3, n, n, n)), b, dx)
     assert np.array_equal(rhs, ref)
     assert np.array_equal(rhs, b)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("where", ["host", "device"])
+def test_newton_solve_guess_one_call(agb, where):
+    """agb_newton_solve_guess equals agb_elastic_learned_guess followed by
+    agb_linear_solve (the same device work in one call)."""
+    from alamo_gb300 import learn
+    n = 33
+    C, F0, bc, dx = P.c1(n)
+    opts = agb.default_opts(precision="mixed", solver="fgmres", bottom_solver="direct", max_coarsening_level=2)
+    with learn.UNet(17, seed=8) as net, agb.Elastic(n, dx, "isotropic", opts) as op:
+        op.SetModel(np.ascontiguousarray(C))
+        op.SetBC(bc)
+        b = op.bc_init()
+        u0, rhs, _, used0 = learn.learned_guess(op, net, b, F0)
+        r0 = agb.Linear(op).solve(u0, rhs, 1e-10, 0.0)
+        if where == "host":
+            u1 = np.full((3, n, n, n), np.nan)
+            r1 = agb.Newton(op).solve_guess(net, u1, b, F0, tol_rel=1e-10, tol_abs=0.0)
+        else:
+            dev = torch.device("cuda", 0)
+            ut = torch.full((3, n, n, n), float("nan"), dtype=torch.float64, device=dev)
+            bt = torch.from_numpy(b).to(dev)
+            Ft = torch.from_numpy(np.ascontiguousarray(F0)).to(dev)
+            P_ = agb.DevicePtr
+            r1 = agb.Newton(op).solve_guess(net, P_(ut.data_ptr()), P_(bt.data_ptr()), (P_(Ft.data_ptr()), 1),
+                                            tol_rel=1e-10, tol_abs=0.0)
+            u1 = ut.cpu().numpy()
+    assert r1["guess_used"] == used0
+    assert r1["iters"] == r0["iters"]
+    assert np.array_equal(u1, u0)
