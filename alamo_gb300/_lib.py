@@ -23,7 +23,7 @@ EXPORTS = [
     "agb_last_error", "agb_version", "agb_residual_norms_noalloc",
     "agb_unet_create", "agb_unet_destroy", "agb_unet_num_params", "agb_unet_get_params", "agb_unet_set_params",
     "agb_unet_train_step", "agb_unet_predict", "agb_elastic_learned_guess", "agb_conv3_bf16",
-    "agb_newton_solve_n", "agb_elastic_set_psi", "agb_newton_solve_guess",
+    "agb_newton_solve_n", "agb_elastic_set_psi", "agb_newton_solve_guess", "agb_elastic_tensor",
 ]
 
 AGB_OK, AGB_NOT_CONVERGED, AGB_NAN, AGB_BAD_ARG, AGB_CUDA_ERROR, AGB_NOT_READY, AGB_OUT_OF_MEMORY, AGB_LIMIT = range(8)

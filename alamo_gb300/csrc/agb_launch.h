@@ -82,6 +82,11 @@ cudaError_t launch_build_rhs(int sym, const double* u, const double* b, const do
 cudaError_t launch_stress_strain(int sym, const double* u, const double* F0, int f0_ncomp, const double* C,
                                  const LevelGeom<double>& G, double* stress, double* strain, double* energy,
                                  cudaStream_t s);
+// Elastic::Stress (which 0: C grad u times psi_avg) / Elastic::Strain (which 1:
+// sym grad u), SoA per component, 6 Voigt (00, 11, 22, 12, 20, 01) or 9
+// row-major components
+cudaError_t launch_op_tensor(int sym, const double* u, const double* C, const LevelGeom<double>& G, int which,
+                             int voigt, double* out, cudaStream_t s);
 
 // Bottom solve on the coarsest level in one thread block: BiCGStab on the
 // diagonally normalised system (the reference's normalize), FP64, followed by

@@ -1615,6 +1615,22 @@ agb_status agb_elastic_stress_strain(agb_elastic* h, const double* u, const doub
     return AGB_OK;
 }
 
+agb_status agb_elastic_tensor(agb_elastic* h, const double* u, int which, int voigt, double* out, int where) {
+    if (!h || !u || !out) return fail(AGB_BAD_ARG, "null argument");
+    if (which != 0 && which != 1) return fail(AGB_BAD_ARG, "which must be 0 (stress) or 1 (strain)");
+    if (!h->model_set) return fail(AGB_NOT_READY, "model not set");
+    const int64_t N = nodes(h);
+    const size_t ob = sizeof(double) * (voigt ? 6 : 9) * N;
+    const void* du = nullptr;
+    void* dout = nullptr;
+    TRY(dev_in(h, 0, u, sizeof(double) * 3 * N, where, &du));
+    TRY(dev_out(h, 1, out, ob, where, &dout));
+    CK(launch_op_tensor(h->sym, (const double*)du, h->L64[0].C, h->L64[0].G, which, voigt ? 1 : 0, (double*)dout,
+                        h->stream));
+    h->launches++;
+    return finish_out(h, out, dout, ob, where);
+}
+
 agb_status agb_profile_enable(agb_elastic* h, int on) {
     if (!h) return fail(AGB_BAD_ARG, "null handle");
     h->prof = on != 0;

@@ -753,6 +753,58 @@ cudaError_t launch_stress_strain(int sym, const double* u, const double* F0, int
     return cudaGetLastError();
 }
 
+// Operator-level Stress / Strain (src/Operator/Elastic.cpp:426-549): which 0
+// sigma = (C grad u) psi_avg, 1 eps = sym grad u; one-sided gradients at the
+// domain boundary.  Output SoA per component (the MultiFab layout): voigt
+// 6 components (00, 11, 22, 12, 20, 01), else 9 row-major.
+template <int SYM>
+__global__ void __launch_bounds__(256) k_op_tensor(const double* __restrict__ u, const double* __restrict__ C,
+                                                   LevelGeom<double> G, int which, int voigt,
+                                                   double* __restrict__ out) {
+    AGB_NODE_INDEX
+    if (!live) return;
+    double g[3][3], t[3][3];
+    grad_at(u, G, i, j, k, id, g);
+    const int64_t N = G.N;
+    if (which == 0) {
+        auto cf = [&](int a) { return C[a * N + id]; };
+        stress_of<double, SYM>(cf, g, t);
+        if (G.psi) {
+            const double pa = psi_avg_of(G, psi_node<double>(G, i, j, k, nullptr));
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int q = 0; q < 3; q++) t[p][q] *= pa;
+        }
+    } else {
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) t[p][q] = 0.5 * (g[p][q] + g[q][p]);
+    }
+    if (voigt) {
+        out[0 * N + id] = t[0][0];
+        out[1 * N + id] = t[1][1];
+        out[2 * N + id] = t[2][2];
+        out[3 * N + id] = t[1][2];
+        out[4 * N + id] = t[2][0];
+        out[5 * N + id] = t[0][1];
+    } else {
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) out[(p * 3 + q) * N + id] = t[p][q];
+    }
+}
+
+cudaError_t launch_op_tensor(int sym, const double* u, const double* C, const LevelGeom<double>& G, int which,
+                             int voigt, double* out, cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
+    if (sym == SYM_ISO) k_op_tensor<SYM_ISO><<<grd, blk, 0, s>>>(u, C, G, which, voigt, out);
+    else k_op_tensor<SYM_MM><<<grd, blk, 0, s>>>(u, C, G, which, voigt, out);
+    return cudaGetLastError();
+}
+
 }  // namespace agb
 
 namespace agb {

@@ -264,6 +264,24 @@ class Elastic:
     def Stress(self, u, F0=None):
         return self.stress_strain(u, F0)[0]
 
+    def OpStress(self, u, voigt=False):
+        """Elastic::Stress (src/Operator/Elastic.cpp:483-549): (C grad u)
+        psi_avg, SoA (6 Voigt or 9 components, nz, ny, nx)."""
+        return self._tensor(u, 0, voigt)
+
+    def OpStrain(self, u, voigt=False):
+        """Elastic::Strain (src/Operator/Elastic.cpp:426-480): sym grad u,
+        SoA (6 Voigt or 9 components, nz, ny, nx)."""
+        return self._tensor(u, 1, voigt)
+
+    def _tensor(self, u, which, voigt):
+        nx, ny, nz = self.n
+        out = np.empty((6 if voigt else 9, nz, ny, nx))
+        pu, wu = _arg(u)
+        po, wo = _arg(out)
+        L.check(L.lib().agb_elastic_tensor(self.h, pu, int(which), int(bool(voigt)), po, _same_where(wu, wo)))
+        return out
+
     def Strain(self, u):
         return self.stress_strain(u)[1]
 

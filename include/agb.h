@@ -224,6 +224,12 @@ agb_status agb_newton_solve_n(agb_elastic* h, double* u, const double* b, const 
  * Outputs may be NULL. */
 agb_status agb_elastic_stress_strain(agb_elastic* h, const double* u, const double* F0, int f0_ncomp,
                                      double* stress, double* strain, double* energy, int where);
+/* Elastic::Stress / Elastic::Strain (src/Operator/Elastic.cpp:426-549) on
+ * the fine level: which 0 gives sigma = (C grad u) psi_avg (psi_avg = 1
+ * without psi), which 1 gives eps = sym grad u; one-sided gradients on the
+ * domain faces.  out is SoA per component (the MultiFab layout): voigt != 0
+ * gives 6 components (00, 11, 22, 12, 20, 01), else 9 row-major. */
+agb_status agb_elastic_tensor(agb_elastic* h, const double* u, int which, int voigt, double* out, int where);
 
 /* ------------------------------------------------ allocation-free call */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -338,3 +338,37 @@ def test_gpu_psi_cleared_restores_fast_path(agb, oracle):
         op.prepareForSolve()
         assert rel(op.Fapply(u), oracle.fapply(C, bt, u, dx)) <= 1e-12
         assert rel(op.Fapply_f32(u.astype(np.float32)), oracle.fapply(C, bt, u, dx)) <= 2e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mm", [False, True])
+def test_gpu_operator_stress_strain(agb, psi_oracle, mm):
+    """Elastic::Stress = (C grad u) psi_avg and Elastic::Strain = sym grad u
+    in the MultiFab layout, 9 components or the reference's Voigt order
+    (00, 11, 22, 12, 20, 01), with and without psi."""
+    n = 17
+    C, F0, bc, dx = P.voronoi_clamp(n) if mm else P.c1(n)
+    u = P.random_field((3, n, n, n), seed=70)
+    psi = psi_random((n - 1,) * 3, 71)
+    stress, strain, _ = psi_oracle.stress_strain(C, None, u, dx)
+    sg = stress.reshape(n, n, n, 3, 3)
+    ep = strain.reshape(n, n, n, 3, 3)
+    avg, _ = node_avg_grad(psi, dx)
+    pa = (1 - SMALL) * avg + SMALL
+    voigt_idx = [(0, 0), (1, 1), (2, 2), (1, 2), (2, 0), (0, 1)]
+    with make_op(agb, C, bc, dx, psi) as op:
+        for use_psi in (True, False):
+            if not use_psi:
+                op.SetPsi(None)
+            scale = pa if use_psi else 1.0
+            s9 = op.OpStress(u)
+            e9 = op.OpStrain(u)
+            s6 = op.OpStress(u, voigt=True)
+            e6 = op.OpStrain(u, voigt=True)
+            for p in range(3):
+                for q in range(3):
+                    assert rel(s9[3 * p + q], sg[..., p, q] * scale) <= 1e-13
+                    assert rel(e9[3 * p + q], ep[..., p, q]) <= 1e-13
+            for c, (p, q) in enumerate(voigt_idx):
+                assert np.array_equal(s6[c], s9[3 * p + q])
+                assert np.array_equal(e6[c], e9[3 * p + q])
