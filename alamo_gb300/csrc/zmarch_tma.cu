@@ -42,15 +42,23 @@ namespace {
 constexpr int TX = 32, TY = 8, NT = TX * TY;
 constexpr int UHX = TX + 2, UHY = TY + 2;
 constexpr int UPL = 3 * UHY * UHX;                // displacement values per staged plane
-constexpr int US = 4;                             // displacement ring slots
 constexpr int U_PER_T = (UPL + NT - 1) / NT;      // cp.async per thread per plane
 constexpr int CBX = 36, CBY = 10;                 // TMA box (x, y) of a stiffness plane
 constexpr int CEL = CBX * CBY;                    // floats per stiffness entry in a slot
-constexpr int CS = 3;                             // stiffness ring slots
 constexpr uint64_t WAIT_NS = 1000000000ull;       // 1 s: a TMA load takes microseconds
 
+// Prefetch distance and ring sizes.  Step k reads planes k-1 (displacement;
+// its own-column stiffness is in registers), k and k+1, and issues plane
+// k+1+DIST; plane k+DIST must have landed before step k+1.  The isotropic
+// planes are small (2 stiffness entries), so one plane of work does not
+// cover a load's latency: they look two planes ahead.  The major-minor
+// planes (21 entries) cover it with one, and two would not fit two blocks
+// per SM in shared memory.
 template <int NC>
 struct ZtSmem {
+    static constexpr int DIST = NC <= 2 ? 2 : 1;
+    static constexpr int CS = 2 + DIST;   // stiffness ring slots
+    static constexpr int US = 3 + DIST;   // displacement ring slots
     static constexpr int slot_bytes = ((NC * CEL * 4 + 127) / 128) * 128;
     static constexpr int c_bytes = CS * slot_bytes;
     static constexpr int u_bytes = US * UPL * 4;
@@ -105,6 +113,11 @@ __device__ __forceinline__ void cp_async4(uint32_t dst, const float* src) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// wait until at most N of this thread's most recent cp.async groups are pending
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 template <int SYM, int MODE>
 __global__ void __launch_bounds__(NT, 2)
@@ -113,6 +126,7 @@ __global__ void __launch_bounds__(NT, 2)
                  int kchunk, int* __restrict__ err) {
     constexpr int NC = SYM == SYM_ISO ? 2 : 21;
     using SM = ZtSmem<NC>;
+    constexpr int CS = SM::CS, US = SM::US, DIST = SM::DIST;
     extern __shared__ unsigned char zt_raw[];
     __shared__ int abort_flag;
     const uint32_t raw = smem_u32(zt_raw);
@@ -145,11 +159,16 @@ __global__ void __launch_bounds__(NT, 2)
         gval[r] = (q < UPL) & (gx < G.nx) & (gy < G.ny);
         goff[r] = p * N + gx + sy * gy;
     }
-    auto issue_u = [&](int kk) {
+    // one commit group per call (planes past the chunk commit an empty
+    // group, so "the DIST-1 most recent groups" always means the planes
+    // issued after the one waited for)
+    auto issue_u = [&](int kk, bool real) {
         const uint32_t dst = us_u32 + (uint32_t)((kk % US) * UPL) * 4u;
+        if (real) {
 #pragma unroll
-        for (int r = 0; r < U_PER_T; r++)
-            if (gval[r]) cp_async4(dst + soff[r] * 4u, x + goff[r] + sz * (int64_t)kk);
+            for (int r = 0; r < U_PER_T; r++)
+                if (gval[r]) cp_async4(dst + soff[r] * 4u, x + goff[r] + sz * (int64_t)kk);
+        }
         cp_async_commit();
     };
     auto issue_c = [&](int kk) {  // one thread
@@ -169,15 +188,25 @@ __global__ void __launch_bounds__(NT, 2)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     __syncthreads();
+    // planes k0-1 .. k0+DIST (plane k0+DIST only if the chunk reaches it)
     int issued = k0 + 1;  // last plane issued (thread 0 uses it on abort)
     if (tid == 0) {
         issue_c(k0 - 1);
         issue_c(k0);
         issue_c(k0 + 1);
     }
-    issue_u(k0 - 1);
-    issue_u(k0);
-    issue_u(k0 + 1);
+    issue_u(k0 - 1, true);
+    issue_u(k0, true);
+    issue_u(k0 + 1, true);
+#pragma unroll
+    for (int d = 2; d <= DIST; d++) {
+        const bool real = k0 + d <= k1;
+        if (real) {
+            if (tid == 0) issue_c(k0 + d);
+            issued = k0 + d;
+        }
+        issue_u(k0 + d, real);
+    }
 
     // one thread waits for the stiffness planes (the block barrier then
     // orders everyone's reads after the completed copies); no thread polls
@@ -191,7 +220,7 @@ __global__ void __launch_bounds__(NT, 2)
             if (err) atomicExch(err, 1);
         }
     }
-    cp_async_wait_all();
+    cp_async_wait_group<DIST - 1>();
     __syncthreads();
     float Cp[NC];
     {
@@ -218,13 +247,17 @@ __global__ void __launch_bounds__(NT, 2)
     load_bd(k0, bq, dq);
 
     for (int k = k0; k < k1 && !abort_flag; k++) {
-        if (k + 2 <= k1) {
-            if (tid == 0) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue_c(k + 2);
+        {
+            const int kn = k + 1 + DIST;
+            const bool real = kn <= k1;
+            if (real) {
+                if (tid == 0) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    issue_c(kn);
+                }
+                issued = kn;
             }
-            issue_u(k + 2);
-            issued = k + 2;
+            issue_u(kn, real);
         }
         const int64_t id = i + sy * j + sz * (int64_t)k;
         float bn[3] = {0.f, 0.f, 0.f}, dn[3] = {1.f, 1.f, 1.f};
@@ -240,9 +273,15 @@ __global__ void __launch_bounds__(NT, 2)
                 const float* s = c == 0 ? u0 : (c < 0 ? um : up);
                 return s[p * (UHY * UHX) + bb * UHX + a];
             };
+            // the own column's stiffness of plane k, read once: the stencil's
+            // centre entries and, for the next step, the plane-below values
+            float c0[NC];
+#pragma unroll
+            for (int e = 0; e < NC; e++) c0[e] = cc[e * CEL];
             auto Cf = [&](int e, int a, int bb, int c) -> float {
                 if (c > 0) return cn[e * CEL];
                 if (c < 0) return Cp[e];
+                if (a == 0 && bb == 0) return c0[e];
                 return cc[e * CEL + bb * CBX + a];
             };
             float r[3];
@@ -260,21 +299,24 @@ __global__ void __launch_bounds__(NT, 2)
                     out[q] = bq[c] - r[c];
                 }
             }
-        }
 #pragma unroll
-        for (int e = 0; e < NC; e++) Cp[e] = cc[e * CEL];
+            for (int e = 0; e < NC; e++) Cp[e] = c0[e];
+        }
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             bq[c] = bn[c];
             dq[c] = dn[c];
         }
-        cp_async_wait_all();
+        // plane k+2 (read by step k+1) must have landed; the DIST-1 newer
+        // planes may still be in flight
+        cp_async_wait_group<DIST - 1>();
         if (tid == 0 && k + 2 <= k1 && !mbar_wait(bar_u32 + 8u * ((k + 2) % CS), parity(k + 2))) {
             abort_flag = 1;
             if (err) atomicExch(err, 1);
         }
         __syncthreads();
     }
+    cp_async_wait_all();
     if (abort_flag && tid == 0) {
         // bounded wait for the TMA loads still in flight (at most the
         // latest load of each slot) before the block gives its shared

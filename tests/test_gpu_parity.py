@@ -213,13 +213,18 @@ def test_zmarch_matches_per_node_kernels(agb, oracle, case):
 
 
 @pytest.mark.parametrize("dims", [(41, 19, 37), (3, 3, 3), (35, 9, 4), (66, 11, 97)])
-def test_zmarch_tma_ragged_grids(agb, oracle, dims):
+@pytest.mark.parametrize("sym", ["mm", "iso"])
+def test_zmarch_tma_ragged_grids(agb, oracle, dims, sym):
     """TMA-staged FP32 Fapply on grids whose interior does not fill the
     32 x 8 tiles or the z chunks (partial tiles, a 1-node interior, a pitch
     that needs padding) against the oracle's FP64 operator, to FP32
-    rounding; random boundary types exercise the separate face kernel."""
+    rounding; random boundary types exercise the separate face kernel.  The
+    isotropic kernel stages two planes ahead, the major-minor one one."""
     nx, ny, nz = dims
-    C = np.ascontiguousarray(agb.synth.voronoi_cubic(max(dims), 16, seed=5)[0][:nz, :ny, :nx])
+    if sym == "mm":
+        C = np.ascontiguousarray(agb.synth.voronoi_cubic(max(dims), 16, seed=5)[0][:nz, :ny, :nx])
+    else:
+        C = np.ascontiguousarray(np.random.default_rng(5).uniform(1.0, 10.0, (nz, ny, nx, 2)))
     bc = P.random_bc(77)
     dx = np.array([1 / (nx - 1), 1 / (ny - 1), 1 / (nz - 1)])
     u = P.random_field((3, nz, ny, nx), 78)
@@ -424,22 +429,33 @@ def test_mixed_matches_fp64_129(agb):
     assert rel(sols[1], sols[0]) <= 1e-7
 
 
-def test_zmarch_tma_repeatable_at_scale(agb):
+@pytest.mark.parametrize("sym", ["mm", "iso"])
+def test_zmarch_tma_repeatable_at_scale(agb, sym):
     """The TMA-staged sweeps at 129^3 (640 blocks, 10 z-chunks) against the
-    one-thread-per-node kernels, five times over: a missing wait or barrier
+    one-thread-per-node kernels, five times over, as Fapply and inside an
+    FP32 V-cycle (the Jacobi and residual forms): a missing wait or barrier
     in the staging pipeline shows up as a run-to-run difference or a wrong
     plane at a chunk boundary."""
-    C = np.ascontiguousarray(agb.synth.voronoi_cubic(129, 64, seed=11)[0])
+    if sym == "mm":
+        C = np.ascontiguousarray(agb.synth.voronoi_cubic(129, 64, seed=11)[0])
+    else:
+        C = np.ascontiguousarray(agb.synth.spheres_diffuse(129, 30, 11, 0.05, 0.12)[0])
     bc = P.random_bc(13)
     dx = 1.0 / 128
-    u = P.random_field((3, 129, 129, 129), 14).astype(np.float32)
+    u = P.random_field((3, 129, 129, 129), 14)
+    u32 = u.astype(np.float32)
     with make_op(agb, C, bc, dx, fine_kernel=1) as op:
-        ref = op.Fapply_f32(u)
+        ref = op.Fapply_f32(u32)
+        vref = op.vcycle(u, precision="mixed")
     with make_op(agb, C, bc, dx, fine_kernel=0) as op:
-        outs = [op.Fapply_f32(u) for _ in range(5)]
+        outs = [op.Fapply_f32(u32) for _ in range(5)]
+        vcs = [op.vcycle(u, precision="mixed") for _ in range(3)]
     for f in outs:
         assert np.array_equal(f, outs[0])
         assert rel(f, ref) <= 2e-6
+    for v in vcs:
+        assert np.array_equal(v, vcs[0])
+        assert rel(v, vref) <= 1e-5
 
 
 def test_newton_iterations_match_oracle_loop(agb, oracle):
