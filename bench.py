@@ -56,8 +56,12 @@ FAMILY = {"fapply_f64": 0, "jacobi_f64": 1, "residual_f64": 2, "fapply_f32": 3, 
 # over 2,146,689 nodes, profiles/k_zmarch_tma_jacobi_mm_129.md; it streams
 # every array once, so it scales with the nodes) and the boundary-face
 # kernel per boundary node (28.1 MB + 0.1 MB over 98,306 boundary nodes,
-# profiles/k_zt_faces_mm_129.md); (per node, per boundary node)
-TRAFFIC_PER_NODE = {("jacobi_f32", 21): ((283.893248e6 + 19.328e6) / 2146689, (28.08704e6 + 0.097536e6) / 98306)}
+# profiles/k_zt_faces_mm_129.md); (per node, per boundary node).  The
+# isotropic sweep's interior from a 257^3 capture (757.9 MB + 183.8 MB over
+# 16,974,593 nodes, profiles/k_zmarch_tma_jacobi_iso_257.md); its faces were
+# not captured (None: the figure is the interior sweep's alone)
+TRAFFIC_PER_NODE = {("jacobi_f32", 21): ((283.893248e6 + 19.328e6) / 2146689, (28.08704e6 + 0.097536e6) / 98306),
+                    ("jacobi_f32", 2): ((757.910784e6 + 183.846656e6) / 16974593, None)}
 
 
 def parse():
@@ -346,7 +350,10 @@ def main():
         traf = TRAFFIC_PER_NODE.get((dom, nc))
         nb = N - (n - 2) ** 3  # boundary nodes
         roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": traf[0] * N + traf[1] * nb if traf else None,
+                "frac": achieved / peaks["hbm_gbs"],
+                "traffic": (traf[0] * N + (traf[1] * nb if traf[1] is not None else 0.0)) if traf else None,
+                "traffic_covers": (("interior sweep and boundary faces" if traf[1] is not None else
+                                    "interior sweep only") if traf else None),
                 "peak_source": peak_kind, "launches": cnt, "avg_launch_ms": ms / cnt,
                 "alg_bytes_per_launch": alg_bytes, "share_of_step": ms / 1e3 / (sec * args.steps)}
     kernels = {k: {"launches": v[0], "ms": v[1]} for k, v in fam.items() if v[0] > 0}
