@@ -39,6 +39,11 @@ cudaError_t launch_vec_norms(const double* v, int64_t n, double* partials, int n
 // nodal full weighting of a 3-component field, fine level -> coarse level
 template <typename T>
 cudaError_t launch_restrict(const T* fine, const LevelGeom<T>& Gf, T* crse, const LevelGeom<T>& Gc, cudaStream_t s);
+// the restriction fused with the coarse level's first Jacobi sweep from a
+// zero correction: xout = omega crse / diag
+template <typename T>
+cudaError_t launch_restrict_jacobi(const T* fine, const LevelGeom<T>& Gf, T* crse, const LevelGeom<T>& Gc,
+                                   const T* diag, T omega, T* xout, cudaStream_t s);
 // same weights on nc stiffness components (SoA)
 cudaError_t launch_restrict_C(const double* Cf, const LevelGeom<double>& Gf, double* Cc, const LevelGeom<double>& Gc,
                               int nc, cudaStream_t s);

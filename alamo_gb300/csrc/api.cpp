@@ -515,7 +515,8 @@ cudaError_t level_zm<double>(agb_elastic* h, const Lev<double>& v, int mode, con
 
 // ncalls Fsmooth calls (2 sweeps each) on level l; cor_zero: cor is known 0
 template <typename T>
-agb_status smooth(agb_elastic* h, std::vector<Lev<T>>& L, int l, int ncalls, bool cor_zero) {
+agb_status smooth(agb_elastic* h, std::vector<Lev<T>>& L, int l, int ncalls, bool cor_zero,
+                  bool first_done = false) {
     Lev<T>& v = L[l];
     const T w = (T)h->opts.omega;
     const int sweeps = 2 * ncalls;
@@ -524,6 +525,11 @@ agb_status smooth(agb_elastic* h, std::vector<Lev<T>>& L, int l, int ncalls, boo
         return AGB_OK;
     }
     for (int s = 0; s < sweeps; s++) {
+        if (s == 0 && cor_zero && first_done) {
+            // the sweep from zero was written into tmp by the restriction
+            std::swap(v.cor, v.tmp);
+            continue;
+        }
         {
             ProfScope ps(h, Fam<T>::J, l == 0 && !(cor_zero && s == 0));
             if (use_zm<T>(h, v, l) && !(cor_zero && s == 0))
@@ -582,9 +588,12 @@ agb_status bottom<float>(agb_elastic* h, std::vector<Lev<float>>& L) {
 template <typename T>
 agb_status vcycle(agb_elastic* h, std::vector<Lev<T>>& L) {
     const int nl = (int)L.size();
+    // levels above the bottom receive their first pre-smoothing sweep (from
+    // a zero correction) from the restriction that fills their right-hand side
+    const bool fuse = h->opts.pre_smooth > 0;
     for (int l = 0; l < nl - 1; l++) {
         Lev<T>& v = L[l];
-        TRY(smooth<T>(h, L, l, h->opts.pre_smooth, true));
+        TRY(smooth<T>(h, L, l, h->opts.pre_smooth, true, fuse && l > 0));
         {
             ProfScope ps(h, Fam<T>::R, l == 0);
             if (use_zm<T>(h, v, l))
@@ -594,7 +603,11 @@ agb_status vcycle(agb_elastic* h, std::vector<Lev<T>>& L) {
         }
         {
             ProfScope ps(h, AGB_K_RESTRICT, l == 0);
-            CK(launch_restrict<T>(v.rescor, v.G, L[l + 1].res, L[l + 1].G, h->stream));
+            Lev<T>& c = L[l + 1];
+            if (fuse && l + 1 < nl - 1)
+                CK(launch_restrict_jacobi<T>(v.rescor, v.G, c.res, c.G, c.diag, (T)h->opts.omega, c.tmp, h->stream));
+            else
+                CK(launch_restrict<T>(v.rescor, v.G, c.res, c.G, h->stream));
         }
         h->launches += 2;
     }

@@ -298,9 +298,12 @@ __device__ __forceinline__ T restrict_point(F f, int I, int J, int K, int ncx, i
     return corners * T(1.0 / 64.0) + edges * T(1.0 / 32.0) + faces * T(1.0 / 16.0) + f(0, 0, 0) * T(1.0 / 8.0);
 }
 
+// xout (optional): the coarse level's first Jacobi sweep from a zero
+// correction, xout = omega crse / diag (k_jacobi_zero fused in)
 template <typename T>
 __global__ void __launch_bounds__(256) k_restrict(const T* __restrict__ fine, LevelGeom<T> Gf, T* __restrict__ crse,
-                                                  LevelGeom<T> G) {
+                                                  LevelGeom<T> G, const T* __restrict__ dg, T omega,
+                                                  T* __restrict__ xout) {
     AGB_NODE_INDEX
     if (!live) return;
     const int64_t fid = 2 * i + Gf.sy * (2 * j) + Gf.sz * (2 * k);
@@ -308,16 +311,31 @@ __global__ void __launch_bounds__(256) k_restrict(const T* __restrict__ fine, Le
     for (int c = 0; c < 3; c++) {
         const T* fc = fine + c * Gf.N + fid;
         auto f = [&](int a, int b, int d) { return fc[a + Gf.sy * b + Gf.sz * d]; };
-        crse[c * G.N + id] = restrict_point<T>(f, i, j, k, G.nx, G.ny, G.nz);
+        const T v = restrict_point<T>(f, i, j, k, G.nx, G.ny, G.nz);
+        crse[c * G.N + id] = v;
+        if (xout) xout[c * G.N + id] = omega * (v - T(0)) / dg[c * G.N + id];
     }
 }
 
 template <typename T>
 cudaError_t launch_restrict(const T* fine, const LevelGeom<T>& Gf, T* crse, const LevelGeom<T>& Gc, cudaStream_t s) {
     dim3 blk(BX, BY, BZ), grd = grid3(Gc.nx, Gc.ny, Gc.nz);
-    k_restrict<T><<<grd, blk, 0, s>>>(fine, Gf, crse, Gc);
+    k_restrict<T><<<grd, blk, 0, s>>>(fine, Gf, crse, Gc, nullptr, T(0), nullptr);
     return cudaGetLastError();
 }
+
+template <typename T>
+cudaError_t launch_restrict_jacobi(const T* fine, const LevelGeom<T>& Gf, T* crse, const LevelGeom<T>& Gc,
+                                   const T* diag, T omega, T* xout, cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(Gc.nx, Gc.ny, Gc.nz);
+    k_restrict<T><<<grd, blk, 0, s>>>(fine, Gf, crse, Gc, diag, omega, xout);
+    return cudaGetLastError();
+}
+template cudaError_t launch_restrict_jacobi<double>(const double*, const LevelGeom<double>&, double*,
+                                                    const LevelGeom<double>&, const double*, double, double*,
+                                                    cudaStream_t);
+template cudaError_t launch_restrict_jacobi<float>(const float*, const LevelGeom<float>&, float*,
+                                                   const LevelGeom<float>&, const float*, float, float*, cudaStream_t);
 template cudaError_t launch_restrict<double>(const double*, const LevelGeom<double>&, double*,
                                              const LevelGeom<double>&, cudaStream_t);
 template cudaError_t launch_restrict<float>(const float*, const LevelGeom<float>&, float*, const LevelGeom<float>&,
