@@ -69,6 +69,8 @@ cudaError_t launch_guess_features(int sym, const double* C, int64_t N, const dou
                                   cudaStream_t s);
 cudaError_t launch_soa_to_aos(const double* soa, double* aos, int64_t N, int nc, cudaStream_t s);
 cudaError_t launch_to_float(const double* in, float* out, int64_t n, double scale, cudaStream_t s);
+// out = 1 / in (FP32)
+cudaError_t launch_recip(const float* in, float* out, int64_t n, cudaStream_t s);
 // out(double) += scale * in(float)
 cudaError_t launch_add_float(const float* in, double* out, int64_t n, double scale, cudaStream_t s);
 cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStream_t s);

@@ -72,6 +72,8 @@ struct Lev {
     // psi of this level (ghosted, LevelGeom::psi layout), owned; the FP64
     // fine level uses the handle's psi_fine instead
     T* psi = nullptr;
+    // 1 / diag of FP32 levels swept by the TMA kernels (their Jacobi form)
+    T* dinv = nullptr;
 };
 
 // Krylov space of the flexible GMRES: Arnoldi basis V (m+1 vectors), the
@@ -213,6 +215,7 @@ void free_levels(std::vector<Lev<T>>& L) {
         cudaFree(l.C); cudaFree(l.diag); cudaFree(l.res); cudaFree(l.cor); cudaFree(l.rescor); cudaFree(l.tmp);
         cudaFree(l.Cpad);
         cudaFree(l.psi);
+        cudaFree(l.dinv);
     }
     L.clear();
 }
@@ -382,7 +385,9 @@ agb_status build_f32(agb_elastic* h) {
             v.tma = false;
         }
         CK(launch_pad_stiffness(v.C, v.Cpad, G.nx, G.ny, G.nz, h->nc, h->stream));
-        h->launches++;
+        if (!v.dinv) CK(cudaMalloc(&v.dinv, sizeof(float) * 3 * G.N));
+        CK(launch_recip(v.diag, v.dinv, 3 * G.N, h->stream));
+        h->launches += 2;
         if (!v.tma) {
             CK(make_stiffness_map(v.Cpad, G.nx, G.ny, G.nz, h->nc, &v.map));
             v.tma = true;
@@ -502,8 +507,9 @@ cudaError_t level_zm<float>(agb_elastic* h, const Lev<float>& v, int mode, const
         // second stream beside the interior sweep measured slower (the face
         // blocks take SM slots the marching blocks need)
         h->launches++;  // interior + faces
-        return launch_zmarch_tma(mode, h->sym, v.map, x, v.C, v.G, h->bc, b, dg, omega, out, h->bottom_info + 3,
-                                 h->stream, nullptr);
+        // the TMA kernels' Jacobi form takes the inverse diagonal
+        return launch_zmarch_tma(mode, h->sym, v.map, x, v.C, v.G, h->bc, b, mode == 1 ? v.dinv : dg, omega, out,
+                                 h->bottom_info + 3, h->stream, nullptr);
     }
     return launch_zmarch<float>(mode, h->sym, x, v.C, v.G, h->bc, b, dg, omega, out, h->stream);
 }

@@ -492,6 +492,16 @@ cudaError_t launch_soa_to_aos(const double* soa, double* aos, int64_t N, int nc,
     return cudaGetLastError();
 }
 
+__global__ void k_recip(const float* __restrict__ in, float* __restrict__ out, int64_t n) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        out[q] = 1.f / in[q];
+}
+
+cudaError_t launch_recip(const float* in, float* out, int64_t n, cudaStream_t s) {
+    k_recip<<<flat_blocks(n), 256, 0, s>>>(in, out, n);
+    return cudaGetLastError();
+}
+
 __global__ void k_to_float(const double* __restrict__ in, float* __restrict__ out, int64_t n, double scale) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
         out[q] = (float)(in[q] * scale);

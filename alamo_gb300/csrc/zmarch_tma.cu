@@ -26,7 +26,10 @@
 // the failure in *err, stops marching (uniformly, through a shared flag),
 // waits (bounded) for its TMA copies still in flight and returns.
 //
-// Epilogues: FAPPLY out = A x; JACOBI one damped-Jacobi sweep; RESIDUAL
+// Epilogues: FAPPLY out = A x; JACOBI one damped-Jacobi sweep, written as
+// x + omega (b - A x) / diag with the inverse diagonal (the reference's
+// (1 - omega) x + omega (b - (A x - x diag)) / diag rearranged: one multiply
+// instead of a division per component in this FP32 preconditioner); RESIDUAL
 // out = b - A x.
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -293,8 +296,7 @@ __global__ void __launch_bounds__(NT, 2)
                     out[q] = r[c];
                 } else if (MODE == 1) {
                     const float xv = u0[c * (UHY * UHX)];
-                    const float rx = r[c] - xv * dq[c];
-                    out[q] = (1.f - omega) * xv + omega * (bq[c] - rx) / dq[c];
+                    out[q] = xv + omega * (bq[c] - r[c]) * dq[c];
                 } else {
                     out[q] = bq[c] - r[c];
                 }
@@ -369,8 +371,8 @@ __global__ void __launch_bounds__(256) k_zt_faces(const float* __restrict__ x, c
         if (MODE == 0) {
             out[q] = r[c];
         } else if (MODE == 1) {
-            const float xv = x[q], d = dg[q];
-            out[q] = (1.f - omega) * xv + omega * (b[q] - (r[c] - xv * d)) / d;
+            const float xv = x[q];
+            out[q] = xv + omega * (b[q] - r[c]) * dg[q];
         } else {
             out[q] = b[q] - r[c];
         }

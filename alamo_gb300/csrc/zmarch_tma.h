@@ -17,7 +17,8 @@ int64_t zmarch_tma_pitch(int nx);
 cudaError_t launch_pad_stiffness(const float* C, float* Cpad, int nx, int ny, int nz, int nc, cudaStream_t s);
 // 4-D tensor map (x, y, z, entry) over the padded copy, box 36 x 10 x 1 x nc
 cudaError_t make_stiffness_map(const float* Cpad, int nx, int ny, int nz, int nc, CUtensorMap* map);
-// mode 0: out = A x; 1: one damped-Jacobi sweep (b, dg, omega); 2: out = b - A x.
+// mode 0: out = A x; 1: one damped-Jacobi sweep (b, dg = the INVERSE diagonal,
+// omega) in the form x + omega (b - A x) / diag; 2: out = b - A x.
 // C is the unpadded FP32 stiffness (boundary faces), map the padded copy's
 // tensor map (interior).  *err is set to 1 when a TMA wait gave up.  The
 // interior kernel goes to s; the boundary-face kernel to s_faces when it is
