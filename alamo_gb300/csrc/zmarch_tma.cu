@@ -165,21 +165,24 @@ __global__ void __launch_bounds__(NT, 2)
     // one commit group per call (planes past the chunk commit an empty
     // group, so "the DIST-1 most recent groups" always means the planes
     // issued after the one waited for)
-    auto issue_u = [&](int kk, bool real) {
-        const uint32_t dst = us_u32 + (uint32_t)((kk % US) * UPL) * 4u;
+    // plane kk into ring slot su (displacement) / s (stiffness)
+    auto issue_u_at = [&](int kk, int su, bool real) {
+        const uint32_t dst = us_u32 + (uint32_t)(su * UPL) * 4u;
         if (real) {
+            const float* xk = x + sz * (int64_t)kk;
 #pragma unroll
             for (int r = 0; r < U_PER_T; r++)
-                if (gval[r]) cp_async4(dst + soff[r] * 4u, x + goff[r] + sz * (int64_t)kk);
+                if (gval[r]) cp_async4(dst + soff[r] * 4u, xk + goff[r]);
         }
         cp_async_commit();
     };
-    auto issue_c = [&](int kk) {  // one thread
-        const int s = kk % CS;
+    auto issue_u = [&](int kk, bool real) { issue_u_at(kk, kk % US, real); };
+    auto issue_c_at = [&](int kk, int s) {  // one thread
         mbar_expect_tx(bar_u32 + 8u * s, SM::box_bytes);
         tma_load_4d(cs_u32 + (uint32_t)(s * SM::slot_bytes), &cmap, TX * blockIdx.x, TY * blockIdx.y, kk, 0,
                     bar_u32 + 8u * s);
     };
+    auto issue_c = [&](int kk) { issue_c_at(kk, kk % CS); };
     // plane kk is the n-th load into its slot, n = (kk - (k0 - 1)) / CS
     auto parity = [&](int kk) { return (uint32_t)(((kk - (k0 - 1)) / CS) & 1); };
     auto cslot = [&](int kk) { return Cs + (kk % CS) * (SM::slot_bytes / 4) + (ty + 1) * CBX + (tx + 1); };
@@ -249,29 +252,47 @@ __global__ void __launch_bounds__(NT, 2)
     };
     load_bd(k0, bq, dq);
 
+    // ring slots advance by one per step.  The major-minor kernel keeps them
+    // as counters (plane k's slots su (displacement) and sc (stiffness), the
+    // slot and mbarrier parity of plane k+2, the plane waited for) -- 1 %
+    // faster; the isotropic kernel measured faster with the modulo
+    // expressions (fewer live registers), so it recomputes them per step.
+    constexpr bool RC = SYM == SYM_MM;
+    auto wrap = [](int v, int n) { return v >= n ? v - n : v; };
+    int su = k0 % US, sc = k0 % CS;
+    int sw = (k0 + 2) % CS;
+    uint32_t pw = parity(k0 + 2);
+    const int sbase = (k0 - 1) % CS;  // a slot's load count grows when the plane index passes it
+    const int o = (ty + 1) * UHX + (tx + 1);
+    const int oc = (ty + 1) * CBX + (tx + 1);
     for (int k = k0; k < k1 && !abort_flag; k++) {
+        if (!RC) {
+            su = k % US;
+            sc = k % CS;
+            sw = (k + 2) % CS;
+            pw = parity(k + 2);
+        }
         {
             const int kn = k + 1 + DIST;
             const bool real = kn <= k1;
             if (real) {
                 if (tid == 0) {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    issue_c(kn);
+                    issue_c_at(kn, wrap(sc + 1 + DIST, CS));
                 }
                 issued = kn;
             }
-            issue_u(kn, real);
+            issue_u_at(kn, wrap(su + 1 + DIST, US), real);
         }
         const int64_t id = i + sy * j + sz * (int64_t)k;
         float bn[3] = {0.f, 0.f, 0.f}, dn[3] = {1.f, 1.f, 1.f};
         load_bd(k + 1, bn, dn);
-        const float* cc = cslot(k);
+        const float* cc = Cs + sc * (SM::slot_bytes / 4) + oc;
         if (col) {
-            const float* cn = cslot(k + 1);
-            const int o = (ty + 1) * UHX + (tx + 1);
-            const float* u0 = Us + (k % US) * UPL + o;
-            const float* um = Us + ((k + US - 1) % US) * UPL + o;
-            const float* up = Us + ((k + 1) % US) * UPL + o;
+            const float* cn = Cs + wrap(sc + 1, CS) * (SM::slot_bytes / 4) + oc;
+            const float* u0 = Us + su * UPL + o;
+            const float* um = Us + wrap(su + US - 1, US) * UPL + o;
+            const float* up = Us + wrap(su + 1, US) * UPL + o;
             auto U = [&](int p, int a, int bb, int c) -> float {
                 const float* s = c == 0 ? u0 : (c < 0 ? um : up);
                 return s[p * (UHY * UHX) + bb * UHX + a];
@@ -312,11 +333,17 @@ __global__ void __launch_bounds__(NT, 2)
         // plane k+2 (read by step k+1) must have landed; the DIST-1 newer
         // planes may still be in flight
         cp_async_wait_group<DIST - 1>();
-        if (tid == 0 && k + 2 <= k1 && !mbar_wait(bar_u32 + 8u * ((k + 2) % CS), parity(k + 2))) {
+        if (tid == 0 && k + 2 <= k1 && !mbar_wait(bar_u32 + 8u * sw, pw)) {
             abort_flag = 1;
             if (err) atomicExch(err, 1);
         }
         __syncthreads();
+        if (RC) {
+            su = wrap(su + 1, US);
+            sc = wrap(sc + 1, CS);
+            sw = wrap(sw + 1, CS);
+            if (sw == sbase) pw ^= 1u;
+        }
     }
     cp_async_wait_all();
     if (abort_flag && tid == 0) {
