@@ -52,7 +52,7 @@ BYTES_PER_NODE = {
 FAMILY = {"fapply_f64": 0, "jacobi_f64": 1, "residual_f64": 2, "fapply_f32": 3, "jacobi_f32": 4, "residual_f32": 5,
           "restrict": 6, "prolong": 7, "bottom": 8}
 # dram__bytes_read.sum + dram__bytes_write.sum of one fine-level Jacobi
-# sweep from 129^3 captures: the interior sweep per node (283.9 MB + 19.3 MB
+# sweep from 129^3 captures: the interior sweep per node (284.7 MB + 20.3 MB
 # over 2,146,689 nodes, profiles/k_zmarch_tma_jacobi_mm_129.md; it streams
 # every array once, so it scales with the nodes) and the boundary-face
 # kernel per boundary node (28.1 MB + 0.1 MB over 98,306 boundary nodes,
@@ -60,7 +60,7 @@ FAMILY = {"fapply_f64": 0, "jacobi_f64": 1, "residual_f64": 2, "fapply_f32": 3, 
 # isotropic sweep's interior from a 257^3 capture (757.9 MB + 183.8 MB over
 # 16,974,593 nodes, profiles/k_zmarch_tma_jacobi_iso_257.md); its faces were
 # not captured (None: the figure is the interior sweep's alone)
-TRAFFIC_PER_NODE = {("jacobi_f32", 21): ((283.893248e6 + 19.328e6) / 2146689, (28.08704e6 + 0.097536e6) / 98306),
+TRAFFIC_PER_NODE = {("jacobi_f32", 21): ((284.697344e6 + 20.251904e6) / 2146689, (28.08704e6 + 0.097536e6) / 98306),
                     ("jacobi_f32", 2): ((757.910784e6 + 183.846656e6) / 16974593, None)}
 
 
