@@ -204,6 +204,22 @@ def cpu_sample(cfg, n_override, C, F0, bc, dx, cycles):
             "fapply_node_updates_per_s": float(n ** 3 / np.median(fap)), "sample_wall_s": time.perf_counter() - t0}
 
 
+def metric_name(n, guess):
+    """The metric string both arms print (the driver pairs them)."""
+    return ("solve time to 1e-8 rel. residual @%d^3: %smixed FP32/FP64 vs plain FP64; Fapply HBM GB/s"
+            % (n, "learned guess + " if guess else ""))
+
+
+def reduce_max(x, dist, device):
+    """x maximised over the ranks of the process group (one replica per GPU;
+    the slowest replica sets the whole job's time).  dist None: one rank."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -221,7 +237,8 @@ def run_reference(args):
             break
     v = float(np.mean(vals))
     r["value"] = v
-    line = {"impl": "reference", "metric": "solve time to 1e-8 rel. residual @%d^3 (%s)" % (n, args.config),
+    guess = bool(args.guess) and os.path.exists(args.guess)
+    line = {"impl": "reference", "metric": metric_name(n, guess),
             "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "config": {"workload": name, "nodes": n ** 3},
@@ -332,10 +349,7 @@ def main():
     sec = e0.elapsed_time(e1) / 1e3 / args.steps
     fam = {k: op.profile_get(v) for k, v in FAMILY.items()}
     op.profile(False)
-    t = torch.tensor([sec], dtype=torch.float64, device=dev)
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    sec = float(t.item())
+    sec = reduce_max(sec, dist, dev)
 
     # dominant fine-level kernel and its roofline
     peaks, peak_kind = measured_peaks()
@@ -385,15 +399,13 @@ def main():
         e1.record(stream)
         barrier()
         wall = (time.perf_counter() - t0) / args.steps
-        te = torch.tensor([wall], dtype=torch.float64, device=dev)
-        if dist is not None:
-            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        wall = reduce_max(wall, dist, dev)
         vec = 3 * N * 8
         # stiffness, b (and F0) in, u out; the guess path's u is output only,
         # the plain Newton step copies its zero u in
         h2d = C.nbytes + (vec if net is not None else 2 * vec) + (F0.nbytes if F0 is not None else 0)
         d2h = vec
-        e2e = {"value": float(te.item()), "unit": "s", "h2d_bytes_per_step": int(h2d),
+        e2e = {"value": wall, "unit": "s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "timing": "host wall clock around synchronous C-ABI calls"}
 
     # plain FP64 V-cycle solve of the same input
@@ -445,8 +457,7 @@ def main():
 
     rep = reports[-1] if reports else {}
     line = {
-        "metric": "solve time to 1e-8 rel. residual @%d^3: %smixed FP32/FP64 vs plain FP64; Fapply HBM GB/s"
-                  % (n, "learned guess + " if net is not None else ""),
+        "metric": metric_name(n, net is not None),
         "value": sec, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-cycle/f64-refinement" if prec else "f64", "data": "synthetic",
