@@ -24,11 +24,12 @@ EXPORTS = [
     "agb_unet_create", "agb_unet_destroy", "agb_unet_num_params", "agb_unet_get_params", "agb_unet_set_params",
     "agb_unet_train_step", "agb_unet_predict", "agb_elastic_learned_guess", "agb_conv3_bf16",
     "agb_newton_solve_n", "agb_elastic_set_psi", "agb_newton_solve_guess", "agb_elastic_tensor",
+    "agb_newton_solve_neohookean",
 ]
 
 AGB_OK, AGB_NOT_CONVERGED, AGB_NAN, AGB_BAD_ARG, AGB_CUDA_ERROR, AGB_NOT_READY, AGB_OUT_OF_MEMORY, AGB_LIMIT = range(8)
 MEM_HOST, MEM_DEVICE = 0, 1
-SYM_ISOTROPIC, SYM_MAJORMINOR = 0, 1
+SYM_ISOTROPIC, SYM_MAJORMINOR, SYM_MAJOR = 0, 1, 2
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 SOLVER_VCYCLE, SOLVER_FGMRES = 0, 1
 BOTTOM_BICGSTAB, BOTTOM_DIRECT, BOTTOM_SMOOTHER = 0, 1, 2

@@ -54,6 +54,14 @@ template <typename T>
 cudaError_t launch_prolong_add(const T* crse, const LevelGeom<T>& Gc, T* fine, const LevelGeom<T>& Gf,
                                cudaStream_t s);
 
+// NeoHookean (Newton.H:144-196, NeoHookean.H:21-121): dw = DW(F) (SoA 9),
+// C = DDW(F) (SoA 45) at F = I + grad u for the model (mu, kappa) SoA
+cudaError_t launch_neohookean(const double* model, const double* u, const LevelGeom<double>& G, double* dw,
+                              double* C, cudaStream_t s);
+// rhs = b - div dw / b - BC(u, grad u, dw) for a given stress field dw (SoA 9)
+cudaError_t launch_rhs_from_dw(const double* u, const double* b, const double* dw, const LevelGeom<double>& G,
+                               const BcTable& bc, double* rhs, cudaStream_t s);
+
 // psi (Elastic::SetPsi / averageDownCoeffs, src/Operator/Elastic.cpp:118-137,
 // 839-905) in the ghosted layout of LevelGeom::psi: the fine level from the
 // caller's cells, and one coarsening

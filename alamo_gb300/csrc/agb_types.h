@@ -11,7 +11,7 @@
 
 namespace agb {
 
-enum { SYM_ISO = 0, SYM_MM = 1 };
+enum { SYM_ISO = 0, SYM_MM = 1, SYM_MAJ = 2 };
 enum { BC_DISP = 0, BC_TRAC = 1, BC_PERIODIC = 2, BC_NEUMANN = 3, BC_NONE = 4 };
 
 // Boundary-condition types: region * 3 + component, region order of the
@@ -45,6 +45,13 @@ struct LevelGeom {
 AGB_HD constexpr int mm_ut(int a, int b) {
     return a <= b ? (a * 11 - a * a) / 2 + b : (b * 11 - b * b) / 2 + a;
 }
+// index of the 45 Major-symmetry entries: upper triangle, row-major, of the
+// symmetric 9 x 9 matrix over the pairs P = 3 i + j (src/Set/Matrix4_Major.H:
+// 274-320)
+AGB_HD constexpr int maj_ut(int P, int Q) {
+    return P <= Q ? P * 9 - P * (P - 1) / 2 + (Q - P) : Q * 9 - Q * (Q - 1) / 2 + (P - Q);
+}
+AGB_HD constexpr int maj_of(int i, int j, int k, int l) { return maj_ut(3 * i + j, 3 * k + l); }
 AGB_HD constexpr int pair_of(int i, int j) {
     return (i == j) ? (i == 0 ? 0 : i == 1 ? 3 : 5) : ((i + j) == 1 ? 1 : (i + j) == 2 ? 2 : 4);
 }

@@ -133,6 +133,8 @@ struct agb_elastic {
     double* psi_fine = nullptr;
     double psi_small = 1e-8;
     bool psi_set = false;
+    // NeoHookean model (mu, kappa) SoA of the finite-deformation Newton path
+    double* nh_model = nullptr;
     Krylov<double> K64;
     Krylov<float> K32;
     // dense direct bottom solve
@@ -367,7 +369,7 @@ agb_status build_f32(agb_elastic* h) {
         const LevelGeom<float>& G = v.G;
         // the z-marching kernels carry no psi terms: psi runs on the per-node ones
         const int64_t min_nodes = h->opts.tma_min_nodes > 0 ? h->opts.tma_min_nodes : TMA_MIN_NODES;
-        const bool want = h->opts.fine_kernel == 0 && !h->psi_set && G.N >= min_nodes &&
+        const bool want = h->opts.fine_kernel == 0 && !h->psi_set && h->sym != SYM_MAJ && G.N >= min_nodes &&
                           zmarch_tma_supported(G.nx, G.ny, G.nz);
         if (!want) {
             cudaFree(v.Cpad);
@@ -491,7 +493,7 @@ template <typename T>
 bool use_zm(const agb_elastic*, const Lev<T>&, int) { return false; }
 template <>
 bool use_zm<float>(const agb_elastic* h, const Lev<float>& v, int l) {
-    if (h->psi_set) return false;
+    if (h->psi_set || h->sym == SYM_MAJ) return false;
     return h->opts.fine_kernel == 0 ? v.tma : (h->opts.fine_kernel == 2 && l == 0);
 }
 
@@ -1019,10 +1021,11 @@ agb_status agb_elastic_create(agb_elastic** out, int nx, int ny, int nz, const d
     *out = nullptr;
     if (nx < 3 || ny < 3 || nz < 3) return fail(AGB_BAD_ARG, "grid needs at least 3 nodes per axis");
     if (!dx || !(dx[0] > 0) || !(dx[1] > 0) || !(dx[2] > 0)) return fail(AGB_BAD_ARG, "dx must be positive");
-    if (sym != AGB_SYM_ISOTROPIC && sym != AGB_SYM_MAJORMINOR) return fail(AGB_BAD_ARG, "unknown symmetry");
+    if (sym != AGB_SYM_ISOTROPIC && sym != AGB_SYM_MAJORMINOR && sym != AGB_SYM_MAJOR)
+        return fail(AGB_BAD_ARG, "unknown symmetry");
     agb_elastic* h = new agb_elastic();
     h->sym = sym;
-    h->nc = sym == AGB_SYM_ISOTROPIC ? 2 : 21;
+    h->nc = sym == AGB_SYM_ISOTROPIC ? 2 : sym == AGB_SYM_MAJORMINOR ? 21 : 45;
     h->n[0] = nx; h->n[1] = ny; h->n[2] = nz;
     for (int d = 0; d < 3; d++) h->dx[d] = dx[d];
     if (opts) {
@@ -1064,6 +1067,7 @@ agb_status agb_elastic_destroy(agb_elastic* h) {
     cudaFree(h->bcval_dev);
     cudaFree(h->dw);
     cudaFree(h->psi_fine);
+    cudaFree(h->nh_model);
     h->K64.release();
     h->K32.release();
     cudaFree(h->bot_inv);
@@ -1483,6 +1487,7 @@ agb_status agb_newton_solve(agb_elastic* h, double* u, const double* b, const do
 // in io[2] (first 3N doubles); io[2] is scratch, slots 1 and 3 untouched.
 static agb_status learned_guess_dev(agb_elastic* h, agb_unet* net, const void* db, const void* dF, int f0_ncomp,
                                     double norms[2], int* used, double** rhs_out) {
+    if (h->sym == SYM_MAJ) return fail(AGB_BAD_ARG, "the learned guess takes isotropic or major-minor models");
     const int ng = unet_grid(net);
     int lg = -1;
     for (int l = 0; l < (int)h->L64.size(); l++) {
@@ -1637,6 +1642,56 @@ agb_status agb_elastic_stress_strain(agb_elastic* h, const double* u, const doub
     }
     CK(cudaStreamSynchronize(h->stream));
     return AGB_OK;
+}
+
+agb_status agb_newton_solve_neohookean(agb_elastic* h, const double* model, double* u, const double* b,
+                                       double tol_rel, double tol_abs, int nriters, double nrtolerance,
+                                       agb_solve_report* rep, double* relnorm, int where) {
+    if (!h || !model || !u || !b) return fail(AGB_BAD_ARG, "null argument");
+    if (h->sym != SYM_MAJ) return fail(AGB_BAD_ARG, "the NeoHookean tangent needs a handle of AGB_SYM_MAJOR");
+    if (nriters < 1) return fail(AGB_BAD_ARG, "nriters must be >= 1");
+    auto t0 = std::chrono::steady_clock::now();
+    const int64_t N = nodes(h);
+    const size_t bytes = sizeof(double) * 3 * N;
+    const void *dm = nullptr, *db = nullptr;
+    void* du = nullptr;
+    // the model as (mu, kappa) SoA, kept on the handle
+    TRY(dev_in(h, 3, model, sizeof(double) * 2 * N, where, &dm));
+    if (!h->nh_model) CK(cudaMalloc(&h->nh_model, sizeof(double) * 2 * N));
+    CK(launch_aos_to_soa((const double*)dm, h->nh_model, N, 2, h->stream));
+    TRY(dev_in(h, 1, b, bytes, where, &db));
+    TRY(dev_out(h, 0, u, bytes, where, &du));
+    if (where == AGB_MEM_HOST) CK(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, h->stream));
+    if (!h->dw) CK(cudaMalloc(&h->dw, sizeof(double) * 9 * N));
+    TRY(ensure_io(h, 2, 2 * bytes));
+    double* rhs = h->io[2];
+    double* dsol = h->io[2] + 3 * N;
+    agb_status st = AGB_OK;
+    double rn = 0.0;
+    for (int it = 0; it < nriters; it++) {
+        // DW and DDW at F = I + grad u; DDW is the operator's stiffness
+        // (Newton.H:193, Elastic::SetModel) and every level is rebuilt
+        CK(launch_neohookean(h->nh_model, (const double*)du, h->L64[0].G, h->dw, h->L64[0].C, h->stream));
+        h->model_set = true;
+        h->prepared = false;
+        h->have_f32 = false;
+        h->bot_src = 0;
+        CK(launch_rhs_from_dw((const double*)du, (const double*)db, h->dw, h->L64[0].G, h->bc, rhs, h->stream));
+        h->launches += 2;
+        CK(cudaMemsetAsync(dsol, 0, bytes, h->stream));
+        st = solve_dev(h, dsol, rhs, tol_rel, tol_abs, rep, true);
+        if (st != AGB_OK && st != AGB_NOT_CONVERGED) return st;
+        double n2[2];
+        TRY(vec_norms(h, dsol, 3 * N, n2));
+        rn = n2[0];
+        CK(launch_axpy(1.0, dsol, (double*)du, 3 * N, h->stream));
+        h->launches++;
+        if (rn < nrtolerance) break;
+    }
+    if (relnorm) *relnorm = rn;
+    TRY(finish_out(h, u, du, bytes, where));
+    if (rep) rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return st;
 }
 
 agb_status agb_elastic_tensor(agb_elastic* h, const double* u, int which, int voigt, double* out, int where) {

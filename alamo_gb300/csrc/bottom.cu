@@ -190,6 +190,9 @@ cudaError_t launch_bottom_bicgstab_ex(int sym, const double* C, const double* di
     if (sym == SYM_ISO)
         k_bottom<SYM_ISO><<<1, BOT_THREADS, 0, s>>>(C, diag, G, bc, rhs, sol, work, max_iter, tol_rel, tol_abs,
                                                      nsmooth_ok, nsmooth_fail, omega, info);
+    else if (sym == SYM_MAJ)
+        k_bottom<SYM_MAJ><<<1, BOT_THREADS, 0, s>>>(C, diag, G, bc, rhs, sol, work, max_iter, tol_rel, tol_abs,
+                                                     nsmooth_ok, nsmooth_fail, omega, info);
     else
         k_bottom<SYM_MM><<<1, BOT_THREADS, 0, s>>>(C, diag, G, bc, rhs, sol, work, max_iter, tol_rel, tol_abs,
                                                     nsmooth_ok, nsmooth_fail, omega, info);
@@ -388,6 +391,7 @@ cudaError_t build_dense_inverse(int sym, const double* C, const double* diag, co
     unsigned* bar = reinterpret_cast<unsigned*>(work + 4 * (int64_t)nb * nb);  // 2 counters
     dim3 grd((unsigned)((G.N + 255) / 256), (unsigned)nb);
     if (sym == SYM_ISO) k_assemble<SYM_ISO><<<grd, 256, 0, s>>>(C, G, bc, E, Acol, nb);
+    else if (sym == SYM_MAJ) k_assemble<SYM_MAJ><<<grd, 256, 0, s>>>(C, G, bc, E, Acol, nb);
     else k_assemble<SYM_MM><<<grd, 256, 0, s>>>(C, G, bc, E, Acol, nb);
     k_gj_init<<<152 * 4, 256, 0, s>>>(Acol, W, nb, used);
     k_pivot_threshold<<<1, 1024, 0, s>>>(diag, nb, 1e-12, tiny);

@@ -66,9 +66,11 @@ cudaError_t launch_fapply(int sym, const T* u, const T* C, const LevelGeom<T>& G
     dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
     if (G.psi) {
         if (sym == SYM_ISO) k_fapply<T, SYM_ISO, true><<<grd, blk, 0, s>>>(u, C, G, bc, f);
+        else if (sym == SYM_MAJ) k_fapply<T, SYM_MAJ, true><<<grd, blk, 0, s>>>(u, C, G, bc, f);
         else k_fapply<T, SYM_MM, true><<<grd, blk, 0, s>>>(u, C, G, bc, f);
     } else {
         if (sym == SYM_ISO) k_fapply<T, SYM_ISO, false><<<grd, blk, 0, s>>>(u, C, G, bc, f);
+        else if (sym == SYM_MAJ) k_fapply<T, SYM_MAJ, false><<<grd, blk, 0, s>>>(u, C, G, bc, f);
         else k_fapply<T, SYM_MM, false><<<grd, blk, 0, s>>>(u, C, G, bc, f);
     }
     return cudaGetLastError();
@@ -94,6 +96,7 @@ template <typename T>
 cudaError_t launch_diagonal(int sym, const T* C, const LevelGeom<T>& G, const BcTable& bc, T* diag, cudaStream_t s) {
     dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
     if (sym == SYM_ISO) k_diag<T, SYM_ISO><<<grd, blk, 0, s>>>(C, G, bc, diag);
+    else if (sym == SYM_MAJ) k_diag<T, SYM_MAJ><<<grd, blk, 0, s>>>(C, G, bc, diag);
     else k_diag<T, SYM_MM><<<grd, blk, 0, s>>>(C, G, bc, diag);
     return cudaGetLastError();
 }
@@ -147,9 +150,11 @@ cudaError_t launch_jacobi(int sym, const T* x, const T* b, const T* diag, const 
     dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
     if (G.psi) {
         if (sym == SYM_ISO) k_jacobi<T, SYM_ISO, true><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
+        else if (sym == SYM_MAJ) k_jacobi<T, SYM_MAJ, true><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
         else k_jacobi<T, SYM_MM, true><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
     } else {
         if (sym == SYM_ISO) k_jacobi<T, SYM_ISO, false><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
+        else if (sym == SYM_MAJ) k_jacobi<T, SYM_MAJ, false><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
         else k_jacobi<T, SYM_MM, false><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega, xout);
     }
     return cudaGetLastError();
@@ -223,9 +228,11 @@ cudaError_t launch_residual(int sym, const T* x, const T* b, const T* C, const L
     if (nblocks_out) *nblocks_out = (int)(grd.x * grd.y * grd.z);
     if (G.psi) {
         if (sym == SYM_ISO) k_residual<T, SYM_ISO, true><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
+        else if (sym == SYM_MAJ) k_residual<T, SYM_MAJ, true><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
         else k_residual<T, SYM_MM, true><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
     } else {
         if (sym == SYM_ISO) k_residual<T, SYM_ISO, false><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
+        else if (sym == SYM_MAJ) k_residual<T, SYM_MAJ, false><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
         else k_residual<T, SYM_MM, false><<<grd, blk, 0, s>>>(x, b, C, G, bc, r, partials);
     }
     return cudaGetLastError();
@@ -481,8 +488,19 @@ cudaError_t launch_guess_features(int sym, const double* C, int64_t N, const dou
     return cudaGetLastError();
 }
 
+// wider records (the 45 Major-symmetry entries): one strided pass
+__global__ void k_aos_to_soa_wide(const double* __restrict__ a, double* __restrict__ s, int64_t N, int nc) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < N * nc; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = q / N, node = q - c * N;
+        s[q] = a[node * nc + c];
+    }
+}
+
 cudaError_t launch_aos_to_soa(const double* aos, double* soa, int64_t N, int nc, cudaStream_t s) {
-    if (nc > 21) return cudaErrorInvalidValue;
+    if (nc > 21) {
+        k_aos_to_soa_wide<<<flat_blocks(N * nc), 256, 0, s>>>(aos, soa, N, nc);
+        return cudaGetLastError();
+    }
     const int64_t tiles = (N + TR_NODES - 1) / TR_NODES;
     k_aos_to_soa<<<(int)(tiles < 152 * 8 ? tiles : 152 * 8), 256, 0, s>>>(aos, soa, N, nc);
     return cudaGetLastError();
@@ -659,15 +677,99 @@ cudaError_t launch_build_rhs(int sym, const double* u, const double* b, const do
     }
     if (u == nullptr) {
         if (sym == SYM_ISO) k_dw<SYM_ISO, true><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
+        else if (sym == SYM_MAJ) k_dw<SYM_MAJ, true><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
         else k_dw<SYM_MM, true><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
     } else {
         if (sym == SYM_ISO) k_dw<SYM_ISO, false><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
+        else if (sym == SYM_MAJ) k_dw<SYM_MAJ, false><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
         else k_dw<SYM_MM, false><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, dw);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (u == nullptr) k_rhs<true><<<grd, blk, 0, s>>>(u, b, dw, G, bc, rhs);
     else k_rhs<false><<<grd, blk, 0, s>>>(u, b, dw, G, bc, rhs);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- NeoHookean
+// Newton::prepareForSolve for Model::Solid::Finite::NeoHookean
+// (src/Solver/Nonlocal/Newton.H:144-196, src/Model/Solid/Finite/NeoHookean.H:
+// 21-121): per node F = I + grad u (one-sided on the faces), dw = DW(F)
+// (SoA 9, row-major) and C = DDW(F) (SoA 45, Major symmetry; every entry is
+// written by both of its index pairs in the reference's loop order, the
+// later one kept).  model: SoA (mu, kappa).
+__global__ void __launch_bounds__(256) k_neohookean(const double* __restrict__ model, const double* __restrict__ u,
+                                                    LevelGeom<double> G, double* __restrict__ dw,
+                                                    double* __restrict__ C) {
+    AGB_NODE_INDEX
+    if (!live) return;
+    const int64_t N = G.N;
+    double F[3][3];
+    grad_at(u, G, i, j, k, id, F);
+#pragma unroll
+    for (int a = 0; a < 3; a++) F[a][a] += 1.0;
+    const double mu = model[id], kappa = model[N + id];
+    // inverse by cofactors, det by the first row
+    const double c00 = F[1][1] * F[2][2] - F[1][2] * F[2][1];
+    const double c01 = F[1][2] * F[2][0] - F[1][0] * F[2][2];
+    const double c02 = F[1][0] * F[2][1] - F[1][1] * F[2][0];
+    const double J = F[0][0] * c00 + F[0][1] * c01 + F[0][2] * c02;
+    const double iJ = 1.0 / J;
+    double FiT[3][3];  // (F^-1)^T
+    FiT[0][0] = c00 * iJ;
+    FiT[0][1] = c01 * iJ;
+    FiT[0][2] = c02 * iJ;
+    FiT[1][0] = (F[0][2] * F[2][1] - F[0][1] * F[2][2]) * iJ;
+    FiT[1][1] = (F[0][0] * F[2][2] - F[0][2] * F[2][0]) * iJ;
+    FiT[1][2] = (F[0][1] * F[2][0] - F[0][0] * F[2][1]) * iJ;
+    FiT[2][0] = (F[0][1] * F[1][2] - F[0][2] * F[1][1]) * iJ;
+    FiT[2][1] = (F[0][2] * F[1][0] - F[0][0] * F[1][2]) * iJ;
+    FiT[2][2] = (F[0][0] * F[1][1] - F[0][1] * F[1][0]) * iJ;
+    double tr = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b2 = 0; b2 < 3; b2++) tr += F[a][b2] * F[a][b2];
+    const double J23 = pow(fabs(J), 2. / 3.);
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b2 = 0; b2 < 3; b2++)
+            dw[(a * 3 + b2) * N + id] =
+                mu * (F[a][b2] / J23 - tr * FiT[a][b2] / (3. * J23)) + kappa * (J - 1) * J * FiT[a][b2];
+#pragma unroll
+    for (int ii = 0; ii < 3; ii++)
+#pragma unroll
+        for (int jj = 0; jj < 3; jj++)
+#pragma unroll
+            for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+                for (int ll = 0; ll < 3; ll++) {
+                    // only the later of the two writes of an entry is kept
+                    if (3 * ii + jj < 3 * kk + ll) continue;
+                    double t1 = 0.0, t2 = 0.0;
+                    if (ii == kk && jj == ll) t1 += 1.0;
+                    t1 -= (2. / 3.) * F[ii][jj] * FiT[kk][ll];
+                    t1 -= (2. / 3.) * FiT[ii][jj] * F[kk][ll];
+                    t1 += (2. / 9.) * tr * FiT[ii][jj] * FiT[kk][ll];
+                    t1 += (1. / 3.) * tr * FiT[ii][ll] * FiT[kk][jj];
+                    t2 += (2. * J - 1.) * FiT[ii][jj] * FiT[kk][ll];
+                    t2 += (1. - J) * FiT[ii][ll] * FiT[kk][jj];
+                    C[maj_of(ii, jj, kk, ll) * N + id] = (mu / J23) * t1 + kappa * J * t2;
+                }
+}
+
+cudaError_t launch_neohookean(const double* model, const double* u, const LevelGeom<double>& G, double* dw,
+                              double* C, cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
+    k_neohookean<<<grd, blk, 0, s>>>(model, u, G, dw, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rhs_from_dw(const double* u, const double* b, const double* dw, const LevelGeom<double>& G,
+                               const BcTable& bc, double* rhs, cudaStream_t s) {
+    dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
+    k_rhs<false><<<grd, blk, 0, s>>>(u, b, dw, G, bc, rhs);
     return cudaGetLastError();
 }
 
@@ -777,6 +879,7 @@ cudaError_t launch_stress_strain(int sym, const double* u, const double* F0, int
                                  cudaStream_t s) {
     dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
     if (sym == SYM_ISO) k_stress_strain<SYM_ISO><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, stress, strain, energy);
+    else if (sym == SYM_MAJ) k_stress_strain<SYM_MAJ><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, stress, strain, energy);
     else k_stress_strain<SYM_MM><<<grd, blk, 0, s>>>(u, F0, f0_ncomp, C, G, stress, strain, energy);
     return cudaGetLastError();
 }
@@ -829,6 +932,7 @@ cudaError_t launch_op_tensor(int sym, const double* u, const double* C, const Le
                              int voigt, double* out, cudaStream_t s) {
     dim3 blk(BX, BY, BZ), grd = grid3(G.nx, G.ny, G.nz);
     if (sym == SYM_ISO) k_op_tensor<SYM_ISO><<<grd, blk, 0, s>>>(u, C, G, which, voigt, out);
+    else if (sym == SYM_MAJ) k_op_tensor<SYM_MAJ><<<grd, blk, 0, s>>>(u, C, G, which, voigt, out);
     else k_op_tensor<SYM_MM><<<grd, blk, 0, s>>>(u, C, G, which, voigt, out);
     return cudaGetLastError();
 }

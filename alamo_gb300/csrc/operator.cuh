@@ -61,6 +61,19 @@ __device__ __forceinline__ void stress_of(CF c, const T g[3][3], T s[3][3]) {
         s[0][1] = s[1][0] = m * (g[0][1] + g[1][0]);
         s[0][2] = s[2][0] = m * (g[0][2] + g[2][0]);
         s[1][2] = s[2][1] = m * (g[1][2] + g[2][1]);
+    } else if (SYM == SYM_MAJ) {
+        // sigma_ij = sum_kl C_ijkl g_kl (src/Set/Matrix4_Major.H:510-523)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                T acc = T(0);
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+#pragma unroll
+                    for (int l = 0; l < 3; l++) acc += c(maj_of(i, j, k, l)) * g[k][l];
+                s[i][j] = acc;
+            }
     } else {
         const T v[6] = {g[0][0], g[0][1] + g[1][0], g[0][2] + g[2][0], g[1][1], g[1][2] + g[2][1], g[2][2]};
         T w[6];
@@ -265,6 +278,45 @@ __device__ __forceinline__ void interior_rows(UA U, CA Cf, const LevelGeom<T>& G
             for (int q = 0; q < 3; q++) t += dm[q] * (g[i][q] + g[q][i]);
             f[i] += t;
         }
+    } else if (SYM == SYM_MAJ) {
+        // f_i = sum_{jkl} C_ijkl u_{k,lj} (src/Set/Matrix4_Major.H:527-541)
+        // with the Hessian pairs (l, j) of component k
+        auto hs = [&](int k, int l, int j) -> T {
+            if (l == j) return H[k][l];
+            const int a = l < j ? l : j, b = l < j ? j : l;
+            return H[k][a == 0 ? (b == 1 ? XY : XZ) : YZ];
+        };
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            T acc = T(0);
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+#pragma unroll
+                    for (int l = 0; l < 3; l++) acc += Cf(maj_of(i, j, k, l), 0, 0, 0) * hs(k, l, j);
+            f[i] = acc;
+        }
+        // grad C term: f_i += sum_q ((d_q C) grad u)_{iq}, d_q C central
+        T col[3][3];
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const int ox = q == 0, oy = q == 1, oz = q == 2;
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                T acc = T(0);
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+#pragma unroll
+                    for (int l = 0; l < 3; l++) {
+                        const int e = maj_of(i, q, k, l);
+                        acc += (Cf(e, ox, oy, oz) - Cf(e, -ox, -oy, -oz)) * g[k][l];
+                    }
+                col[q][i] = acc * G.h[q];
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 3; i++) f[i] += (col[0][i] + col[1][i]) + col[2][i];
     } else {
         T d[21];
 #pragma unroll
@@ -382,6 +434,14 @@ __device__ __forceinline__ void diag_node(const T* __restrict__ C, const LevelGe
             const T s2 = -(G.i2[0] + G.i2[1] + G.i2[2]) * T(2);
 #pragma unroll
             for (int p = 0; p < 3; p++) dg[p] = m * s2 + (l + m) * (T(-2) * G.i2[p]);
+        } else if (SYM == SYM_MAJ) {
+#pragma unroll
+            for (int p = 0; p < 3; p++) {
+                T acc = T(0);
+#pragma unroll
+                for (int l = 0; l < 3; l++) acc += cf(maj_of(p, l, p, l)) * (T(-2) * G.i2[l]);
+                dg[p] = acc;
+            }
         } else {
 #pragma unroll
             for (int p = 0; p < 3; p++) {

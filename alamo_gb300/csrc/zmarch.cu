@@ -143,6 +143,7 @@ static int zm_kchunk(int nz) { return nz >= 64 ? 32 : 16; }
 template <typename T>
 cudaError_t launch_zmarch(int mode, int sym, const T* x, const T* C, const LevelGeom<T>& G, const BcTable& bc,
                           const T* b, const T* dg, T omega, T* out, cudaStream_t s) {
+    if (sym == SYM_MAJ) return cudaErrorInvalidValue;  // per-node kernels only
     const int kc = zm_kchunk(G.nz);
     dim3 blk(ZX, ZY, 1), grd((G.nx + ZX - 1) / ZX, (G.ny + ZY - 1) / ZY, (G.nz + kc - 1) / kc);
 #define AGB_ZM_CASE(SY, MO) \

@@ -500,7 +500,7 @@ static cudaError_t zt_launch(const CUtensorMap& map, const float* x, const float
 cudaError_t launch_zmarch_tma(int mode, int sym, const CUtensorMap& map, const float* x, const float* C,
                               const LevelGeom<float>& G, const BcTable& bc, const float* b, const float* dg,
                               float omega, float* out, int* err, cudaStream_t s, cudaStream_t s_faces) {
-    if (!zmarch_tma_supported(G.nx, G.ny, G.nz)) return cudaErrorInvalidValue;
+    if (!zmarch_tma_supported(G.nx, G.ny, G.nz) || sym == SYM_MAJ) return cudaErrorInvalidValue;
     if (sym == SYM_ISO) {
         if (mode == 0) return zt_launch<SYM_ISO, 0>(map, x, C, G, bc, b, dg, omega, out, err, s, s_faces);
         if (mode == 1) return zt_launch<SYM_ISO, 1>(map, x, C, G, bc, b, dg, omega, out, err, s, s_faces);

@@ -68,8 +68,8 @@ class Elastic:
         self.n = tuple(int(v) for v in n)
         dxa = np.ascontiguousarray(np.broadcast_to(np.asarray(dx, dtype=np.float64), (3,)))
         self.dx = dxa
-        self.sym = {"isotropic": L.SYM_ISOTROPIC, "majorminor": L.SYM_MAJORMINOR}.get(sym, sym)
-        self.nc = 2 if self.sym == L.SYM_ISOTROPIC else 21
+        self.sym = {"isotropic": L.SYM_ISOTROPIC, "majorminor": L.SYM_MAJORMINOR, "major": L.SYM_MAJOR}.get(sym, sym)
+        self.nc = {L.SYM_ISOTROPIC: 2, L.SYM_MAJORMINOR: 21, L.SYM_MAJOR: 45}[self.sym]
         self.opts = opts if opts is not None else default_opts()
         h = ctypes.c_void_p()
         L.check(L.lib().agb_elastic_create(ctypes.byref(h), self.n[0], self.n[1], self.n[2],
@@ -382,6 +382,25 @@ class Newton(Linear):
         d = rep.as_dict()
         if rn is not None:
             d["relnorm"] = rn
+        return d
+
+    def solve_neohookean(self, model, u, b, tol_rel=1e-8, tol_abs=0.0, allow_not_converged=False):
+        """Newton iterations for a NeoHookean medium (agb_newton_solve_neohookean):
+        model (nz, ny, nx, 2) = (mu, kappa) per node; u in/out.  The handle
+        must be of symmetry "major".  Returns the last linear solve's report
+        plus "relnorm" (max |increment| of the last iteration)."""
+        rep = L.SolveReport()
+        pm, wm = _arg(model)
+        pu, wu = _arg(u)
+        pb, wb = _arg(b)
+        r = ctypes.c_double()
+        st = L.lib().agb_newton_solve_neohookean(self.op.h, pm, pu, pb, ctypes.c_double(tol_rel),
+                                                 ctypes.c_double(tol_abs), self.nriters,
+                                                 ctypes.c_double(self.nrtolerance), ctypes.byref(rep), ctypes.byref(r),
+                                                 _same_where(wm, wu, wb))
+        L.check(st, (L.AGB_OK, L.AGB_NOT_CONVERGED) if allow_not_converged else (L.AGB_OK,))
+        d = rep.as_dict()
+        d["relnorm"] = r.value
         return d
 
     def solve_guess(self, net, u, b, F0=None, tol_rel=1e-8, tol_abs=0.0, allow_not_converged=False):

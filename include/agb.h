@@ -43,7 +43,10 @@ typedef enum {
     AGB_LIMIT = 7          /* request beyond a documented size limit */
 } agb_status;
 
-typedef enum { AGB_SYM_ISOTROPIC = 0, AGB_SYM_MAJORMINOR = 1 } agb_sym;
+/* Set::Sym: Isotropic (2 values per node: lambda, mu), MajorMinor (21,
+ * src/Set/Matrix4_MajorMinor.H:327-375), Major (45, the finite-deformation
+ * tangent, src/Set/Matrix4_Major.H:274-320; per-node kernels only) */
+typedef enum { AGB_SYM_ISOTROPIC = 0, AGB_SYM_MAJORMINOR = 1, AGB_SYM_MAJOR = 2 } agb_sym;
 typedef enum { AGB_MEM_HOST = 0, AGB_MEM_DEVICE = 1 } agb_mem;
 /* BC::Operator::Elastic::Elastic::Type (src/BC/Operator/Elastic/Elastic.H:26) */
 typedef enum {
@@ -224,6 +227,17 @@ agb_status agb_newton_solve_n(agb_elastic* h, double* u, const double* b, const 
  * Outputs may be NULL. */
 agb_status agb_elastic_stress_strain(agb_elastic* h, const double* u, const double* F0, int f0_ncomp,
                                      double* stress, double* strain, double* energy, int where);
+/* Newton::solve (src/Solver/Nonlocal/Newton.H:144-196, 279-358) for
+ * Model::Solid::Finite::NeoHookean (src/Model/Solid/Finite/NeoHookean.H:
+ * 21-121) on a handle of AGB_SYM_MAJOR: up to nriters iterations of
+ * F = I + grad u, dw = DW(F), DDW(F) as the operator's stiffness (every
+ * multigrid level rebuilt), rhs = b - div dw / b - BC(u, grad u, dw), the
+ * increment solved from zero with the handle's solver options, u += it;
+ * stops when max |increment| < nrtolerance (relnorm: that norm).  model:
+ * (mu, kappa) per node, AoS; u in/out. */
+agb_status agb_newton_solve_neohookean(agb_elastic* h, const double* model, double* u, const double* b,
+                                       double tol_rel, double tol_abs, int nriters, double nrtolerance,
+                                       agb_solve_report* rep, double* relnorm, int where);
 /* Elastic::Stress / Elastic::Strain (src/Operator/Elastic.cpp:426-549) on
  * the fine level: which 0 gives sigma = (C grad u) psi_avg (psi_avg = 1
  * without psi), which 1 gives eps = sym grad u; one-sided gradients on the

@@ -66,7 +66,7 @@
 
 namespace {
 
-enum { ISO = 0, MM = 1 };
+enum { ISO = 0, MM = 1, MAJ = 2 };
 enum { DISP = 0, TRAC = 1, PERIODIC = 2, NEUMANN = 3, NONE = 4 };
 enum Sten { LO = 0, HI = 1, CENTRAL = 2 };
 
@@ -101,7 +101,7 @@ struct Grid {
     }
 };
 
-inline int nc_of(int sym) { return sym == ISO ? 2 : 21; }
+inline int nc_of(int sym) { return sym == ISO ? 2 : sym == MM ? 21 : 45; }
 
 // ---------------------------------------------------------------------------
 // Stiffness tensors.  Major-minor storage: 6x6 symmetric matrix over the pair
@@ -120,6 +120,14 @@ struct UTInit {
 
 inline double mm_get(const double* d, int i, int j, int k, int l) { return d[UT[PAIR[i][j]][PAIR[k][l]]]; }
 
+// Major symmetry only (C_ijkl = C_klij): 9x9 symmetric matrix over the pairs
+// P = 3i + j, upper triangle row-major = data[0..44] (Matrix4_Major.H:274-320)
+inline int maj_index(int P, int Q) {
+    if (P > Q) { const int t = P; P = Q; Q = t; }
+    return P * 9 - P * (P - 1) / 2 + (Q - P);
+}
+inline double maj_get(const double* d, int i, int j, int k, int l) { return d[maj_index(3 * i + j, 3 * k + l)]; }
+
 // sigma = C * g  (Matrix4_Isotropic.H:137-157, Matrix4_MajorMinor.H:675-691)
 inline void c_grad(int sym, const double* c, const double g[3][3], double s[3][3]) {
     if (sym == ISO) {
@@ -130,6 +138,15 @@ inline void c_grad(int sym, const double* c, const double g[3][3], double s[3][3
         s[1][2] = m * (g[1][2] + g[2][1]); s[2][1] = s[1][2];
         s[2][0] = m * (g[2][0] + g[0][2]); s[0][2] = s[2][0];
         s[0][1] = m * (g[0][1] + g[1][0]); s[1][0] = s[0][1];
+    } else if (sym == MAJ) {
+        // sigma_ij = sum_kl C(3i+j, 3k+l) g_kl (Matrix4_Major.H:510-523)
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double acc = 0.0;
+                for (int k = 0; k < 3; k++)
+                    for (int l = 0; l < 3; l++) acc += maj_get(c, i, j, k, l) * g[k][l];
+                s[i][j] = acc;
+            }
     } else {
         // symmetric-pair vector of g: (g00, g01+g10, g02+g20, g11, g12+g21, g22)
         const double v[6] = {g[0][0], g[0][1] + g[1][0], g[0][2] + g[2][0], g[1][1], g[1][2] + g[2][1], g[2][2]};
@@ -155,11 +172,13 @@ inline void c_hess(int sym, const double* c, const double b[3][3][3], double f[3
             f[i] = r;
         }
     } else {
+        // Matrix4_Major.H:527-541 / Matrix4_MajorMinor.H:709-767
         for (int i = 0; i < 3; i++) {
             double r = 0.0;
             for (int j = 0; j < 3; j++)
                 for (int k = 0; k < 3; k++)
-                    for (int l = 0; l < 3; l++) r += mm_get(c, i, j, k, l) * b[k][l][j];
+                    for (int l = 0; l < 3; l++)
+                        r += (sym == MAJ ? maj_get(c, i, j, k, l) : mm_get(c, i, j, k, l)) * b[k][l][j];
             f[i] = r;
         }
     }
@@ -351,7 +370,7 @@ void fapply_gradc(int sym, const Grid& g, const double* C, const double gu[3][3]
     for (int q = 0; q < 3; q++) {
         const double* cp = C + g.id(i + E[q][0], j + E[q][1], k + E[q][2]) * nc;
         const double* cm = C + g.id(i - E[q][0], j - E[q][1], k - E[q][2]) * nc;
-        double dc[21];
+        double dc[45];
         for (int a = 0; a < nc; a++) dc[a] = (cp[a] - cm[a]) * 0.5 / g.dx[q];
         double t[3][3];
         c_grad(sym, dc, gu, t);
@@ -759,6 +778,9 @@ void orc_bc_init(int nx, int ny, int nz, const int* bc_type, const double* bc_va
 // (Newton.H:144-231, psi unset):  dw = C (grad u - F0);  rhs = b - div dw in
 // the interior, rhs = b - BC(u, grad u, dw) on the boundary.
 // F0 has f0_ncomp values per node: 0 (none), 1 (F0 = s I) or 9 (row-major).
+void rhs_from_dw(const Grid& g, const double* dw, const int* bc_type, const double* u, const double* b,
+                 double* rhs);
+
 void orc_build_rhs(int sym, int nx, int ny, int nz, const double* dx, const double* C, const double* F0,
                    int f0_ncomp, const int* bc_type, const double* u, const double* b, double* rhs) {
     Grid g = mkgrid(nx, ny, nz, dx);
@@ -784,6 +806,15 @@ void orc_build_rhs(int sym, int nx, int ny, int nz, const double* dx, const doub
         for (int p = 0; p < 3; p++)
             for (int q = 0; q < 3; q++) dw[id * 9 + p * 3 + q] = sg[p][q];
     });
+    rhs_from_dw(g, dw.data(), bc_type, u, b, rhs);
+}
+
+// rhs = b - div(dw) (interior) / b - BC(u, grad u, dw) (boundary) for a given
+// nodal stress field dw (Newton.H:205-266); dw AoS, 9 values row-major
+void rhs_from_dw(const Grid& g, const double* dw, const int* bc_type, const double* u, const double* b,
+                 double* rhs) {
+    const int64_t N = g.N();
+    const double* uu[3] = {u, u + N, u + 2 * N};
     for_nodes(g, [&](int i, int j, int k) {
         const int64_t id = g.id(i, j, k);
         int s[3];
@@ -1244,6 +1275,94 @@ int orc_solve(int sym, int nx, int ny, int nz, const double* dx, const double* C
         rep->setup_seconds = t_setup;
     }
     return status;
+}
+
+}  // extern "C"
+
+
+// ---------------------------------------------------------------------------
+// Model::Solid::Finite::NeoHookean (src/Model/Solid/Finite/NeoHookean.H:21-121):
+// W(F) = mu/2 (tr(F F^T) / J^(2/3) - 3) + kappa/2 (J - 1)^2, DW, DDW (Major
+// symmetry, 45 values written in the reference's loop order).
+// ---------------------------------------------------------------------------
+static void inv3(const double F[3][3], double* J, double Fi[3][3]) {
+    const double c00 = F[1][1] * F[2][2] - F[1][2] * F[2][1];
+    const double c01 = F[1][2] * F[2][0] - F[1][0] * F[2][2];
+    const double c02 = F[1][0] * F[2][1] - F[1][1] * F[2][0];
+    const double det = F[0][0] * c00 + F[0][1] * c01 + F[0][2] * c02;
+    const double id = 1.0 / det;
+    Fi[0][0] = c00 * id;
+    Fi[1][0] = c01 * id;
+    Fi[2][0] = c02 * id;
+    Fi[0][1] = (F[0][2] * F[2][1] - F[0][1] * F[2][2]) * id;
+    Fi[1][1] = (F[0][0] * F[2][2] - F[0][2] * F[2][0]) * id;
+    Fi[2][1] = (F[0][1] * F[2][0] - F[0][0] * F[2][1]) * id;
+    Fi[0][2] = (F[0][1] * F[1][2] - F[0][2] * F[1][1]) * id;
+    Fi[1][2] = (F[0][2] * F[1][0] - F[0][0] * F[1][2]) * id;
+    Fi[2][2] = (F[0][0] * F[1][1] - F[0][1] * F[1][0]) * id;
+    *J = det;
+}
+
+extern "C" {
+
+void orc_neohookean(double mu, double kappa, const double* F9, double* W, double* dw9, double* ddw45) {
+    double F[3][3], Fi[3][3], J;
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) F[a][b] = F9[3 * a + b];
+    inv3(F, &J, Fi);
+    double FinvT[3][3];
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) FinvT[a][b] = Fi[b][a];
+    double tr = 0.0;  // tr(F F^T)
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) tr += F[a][b] * F[a][b];
+    const double J23 = std::pow(std::fabs(J), 2. / 3.);
+    if (W) *W = 0.5 * mu * (tr / J23 - 3.) + 0.5 * kappa * (J - 1.0) * (J - 1.0);
+    if (dw9)
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++)
+                dw9[3 * a + b] = mu * (F[a][b] / J23 - tr * FinvT[a][b] / (3. * J23)) + kappa * (J - 1) * J * FinvT[a][b];
+    if (ddw45)
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++)
+                for (int k = 0; k < 3; k++)
+                    for (int l = 0; l < 3; l++) {
+                        double t1 = 0.0, t2 = 0.0;
+                        if (i == k && j == l) t1 += 1.0;
+                        t1 -= (2. / 3.) * F[i][j] * FinvT[k][l];
+                        t1 -= (2. / 3.) * FinvT[i][j] * F[k][l];
+                        t1 += (2. / 9.) * tr * FinvT[i][j] * FinvT[k][l];
+                        t1 += (1. / 3.) * tr * FinvT[i][l] * FinvT[k][j];
+                        t2 += (2. * J - 1.) * FinvT[i][j] * FinvT[k][l];
+                        t2 += (1. - J) * FinvT[i][l] * FinvT[k][j];
+                        ddw45[maj_index(3 * i + j, 3 * k + l)] = (mu / J23) * t1 + kappa * J * t2;
+                    }
+}
+
+// Newton::prepareForSolve for a NeoHookean medium (Newton.H:144-196): per
+// node F = I + grad u (one-sided on the faces), dw = DW(F) (AoS, 9) and
+// ddw = DDW(F) (AoS, 45); model = (mu, kappa) per node
+void orc_neohookean_field(int nx, int ny, int nz, const double* dx, const double* model, const double* u, double* dw,
+                          double* ddw) {
+    Grid g = mkgrid(nx, ny, nz, dx);
+    const int64_t N = g.N();
+    const double* uu[3] = {u, u + N, u + 2 * N};
+    for_nodes(g, [&](int i, int j, int k) {
+        const int64_t id = g.id(i, j, k);
+        int st[3];
+        get_stencil(g, i, j, k, st);
+        double F[9];
+        for (int p = 0; p < 3; p++)
+            for (int q = 0; q < 3; q++) F[3 * p + q] = d1(g, uu[p], i, j, k, q, st[q]) + (p == q ? 1.0 : 0.0);
+        orc_neohookean(model[2 * id], model[2 * id + 1], F, nullptr, dw + 9 * id, ddw + 45 * id);
+    });
+}
+
+// rhs = b - div(dw) / b - BC(u, grad u, dw) for a given stress field dw (AoS, 9)
+void orc_rhs_dw(int nx, int ny, int nz, const double* dx, const double* dw, const int* bc_type, const double* u,
+                const double* b, double* rhs) {
+    Grid g = mkgrid(nx, ny, nz, dx);
+    rhs_from_dw(g, dw, bc_type, u, b, rhs);
 }
 
 }  // extern "C"

@@ -19,7 +19,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 _lib = None
 
-ISO, MM = 0, 1
+ISO, MM, MAJ = 0, 1, 2
 
 
 class Opts(ctypes.Structure):
@@ -103,7 +103,7 @@ def _dims(u_or_C, vector=True):
 
 
 def sym_of(C):
-    return ISO if C.shape[-1] == 2 else MM
+    return {2: ISO, 21: MM, 45: MAJ}[C.shape[-1]]
 
 
 def set_threads(n):
@@ -166,7 +166,7 @@ def restrict(fine):
 def restrict_C(Cf):
     nzf, nyf, nxf, nc = Cf.shape
     Cc = np.empty(((nzf - 1) // 2 + 1, (nyf - 1) // 2 + 1, (nxf - 1) // 2 + 1, nc))
-    lib().orc_restrict_C(ISO if nc == 2 else MM, nxf, nyf, nzf, _p(Cf), _p(Cc))
+    lib().orc_restrict_C({2: ISO, 21: MM, 45: MAJ}[nc], nxf, nyf, nzf, _p(Cf), _p(Cc))
     return Cc
 
 
@@ -311,3 +311,38 @@ def coarsen_psi(psi_cells):
     lib().orc_coarsen_psi.restype = None
     lib().orc_coarsen_psi(nx, ny, nz, _p(g), _p(out))
     return out[1:-1, 1:-1, 1:-1].copy()
+
+
+def neohookean(mu, kappa, F):
+    """Model::Solid::Finite::NeoHookean at one F: (W, DW (3, 3), DDW (45,))."""
+    F = np.ascontiguousarray(F, dtype=np.float64).reshape(9)
+    W = ctypes.c_double()
+    dw = np.empty(9)
+    ddw = np.empty(45)
+    lib().orc_neohookean.restype = None
+    lib().orc_neohookean(ctypes.c_double(mu), ctypes.c_double(kappa), _p(F), ctypes.byref(W), _p(dw), _p(ddw))
+    return W.value, dw.reshape(3, 3), ddw
+
+
+def neohookean_field(model, u, dx):
+    """dw (nz, ny, nx, 9) and ddw (nz, ny, nx, 45) at F = I + grad u for a
+    per-node (mu, kappa) model (nz, ny, nx, 2)."""
+    nz, ny, nx = model.shape[:3]
+    dw = np.empty((nz, ny, nx, 9))
+    ddw = np.empty((nz, ny, nx, 45))
+    d = _dx(dx)
+    lib().orc_neohookean_field.restype = None
+    lib().orc_neohookean_field(nx, ny, nz, _p(d), _p(np.ascontiguousarray(model)), _p(np.ascontiguousarray(u)),
+                               _p(dw), _p(ddw))
+    return dw, ddw
+
+
+def rhs_dw(dw, bc_type, u, b, dx):
+    """b - div(dw) / b - BC(u, grad u, dw) for a nodal stress field dw."""
+    nz, ny, nx = dw.shape[:3]
+    rhs = np.empty_like(u)
+    d, bt = _dx(dx), _bct(bc_type)
+    lib().orc_rhs_dw.restype = None
+    lib().orc_rhs_dw(nx, ny, nz, _p(d), _p(np.ascontiguousarray(dw)), _p(bt), _p(np.ascontiguousarray(u)),
+                     _p(np.ascontiguousarray(b)), _p(rhs))
+    return rhs
