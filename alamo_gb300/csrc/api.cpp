@@ -806,8 +806,12 @@ agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, doub
 // Linear::solve on device pointers.
 // x_zero: x is known to be 0 on entry, so the initial residual is rhs itself
 // (b - A 0 = b exactly) and is copied instead of computed
+// r32_init (mixed precision, x not zero): the FP32 residual of x already
+// computed on the fine FP32 level (the learned guess's fallback test); the
+// first refinement step starts from it instead of an FP64 residual, and
+// convergence is only declared on an FP64 residual
 agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_rel, double tol_abs,
-                     agb_solve_report* rep, bool x_zero = false) {
+                     agb_solve_report* rep, bool x_zero = false, const float* r32_init = nullptr) {
     auto t0 = std::chrono::steady_clock::now();
     const bool mixed = h->opts.precision == AGB_PRECISION_MIXED;
     // the mixed solve needs the FP32 hierarchy and the fine FP64 stiffness
@@ -826,10 +830,17 @@ agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_re
         x_zero = xn[0] == 0.0;
     }
     int fp64_res = 0;
+    bool r_exact = true;  // r is an FP64 residual (or rhs itself)
     if (x_zero) {
         CK(cudaMemcpyAsync(top.res, rhs, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
         r[0] = bn[0];
         r[1] = bn[1];
+    } else if (mixed && r32_init) {
+        CK(cudaMemsetAsync(top.res, 0, sizeof(double) * n3, h->stream));
+        CK(launch_add_float(r32_init, top.res, n3, 1.0, h->stream));
+        h->launches++;
+        TRY(vec_norms(h, top.res, n3, r));
+        r_exact = false;
     } else {
         TRY(residual64(h, x, rhs, r));
         fp64_res = 1;
@@ -841,7 +852,7 @@ agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_re
     const int maxit = fixed ? h->opts.fixed_iter : h->opts.max_iter;
     int status = AGB_NOT_CONVERGED, it = 0;
     if (std::isnan(r[0]) || std::isnan(r[1])) status = AGB_NAN;
-    else if (r[0] <= target && !fixed) status = AGB_OK;
+    else if (r[0] <= target && !fixed && r_exact) status = AGB_OK;
     else {
         while (it < maxit) {
             if (h->opts.solver == AGB_SOLVER_FGMRES) {
@@ -1605,7 +1616,10 @@ agb_status agb_newton_solve_guess(agb_elastic* h, agb_unet* net, double* u, cons
     TRY(learned_guess_dev(h, net, db, dF, f0_ncomp, nullptr, &ok, &rhs0));
     if (used) *used = ok;
     CK(cudaMemcpyAsync(du, h->L64[0].cor, bytes, cudaMemcpyDeviceToDevice, h->stream));
-    const agb_status st = solve_dev(h, (double*)du, rhs0, tol_rel, tol_abs, rep, ok == 0);
+    // a kept guess's FP32 residual (the fallback test's) starts the mixed
+    // refinement; the FP64 residuals after each inner solve decide
+    const float* r32 = (ok && h->opts.precision == AGB_PRECISION_MIXED) ? h->L32[0].rescor : nullptr;
+    const agb_status st = solve_dev(h, (double*)du, rhs0, tol_rel, tol_abs, rep, ok == 0, r32);
     if (st != AGB_OK && st != AGB_NOT_CONVERGED) return st;
     TRY(finish_out(h, u, du, bytes, where));
     if (rep) rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

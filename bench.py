@@ -310,19 +310,16 @@ def main():
         net = learn.UNet(65)
         net.load(args.guess)
 
-    rhs_dev = torch.zeros_like(u_dev) if net is not None else None
-    linear = A.Linear(op)
 
     def step():
         op.SetModel(P(C_dev.data_ptr()))
         if net is not None:
             # learned initial guess with its residual-based fallback (zero
             # when the fallback fires) as the first iterate of the Newton
-            # step's linear solve
-            _, _, norms, used = learn.learned_guess(op, net, P(b_dev.data_ptr()), F0arg, P(u_dev.data_ptr()),
-                                                    P(rhs_dev.data_ptr()))
-            guesses.append({"used": used, "rhs_guess": norms[0], "rhs_zero": norms[1]})
-            reports.append(linear.solve(P(u_dev.data_ptr()), P(rhs_dev.data_ptr()), 1e-8, 0.0))
+            # step's linear solve, in one call
+            r = newton.solve_guess(net, P(u_dev.data_ptr()), P(b_dev.data_ptr()), F0arg, tol_rel=1e-8, tol_abs=0.0)
+            guesses.append({"used": r["guess_used"]})
+            reports.append(r)
         else:
             with torch.cuda.stream(stream):
                 u_dev.zero_()
@@ -468,9 +465,7 @@ def main():
                    "l2": "inputs larger than L2 (%.1f GB of stiffness)" % (C.nbytes / 1e9)},
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": ck,
         "guess": ({"weights": os.path.relpath(args.guess, ROOT), "network_grid": 65,
-                   "used_fraction": float(np.mean([g["used"] for g in guesses])) if guesses else None,
-                   "restricted_rhs_at_guess": guesses[-1]["rhs_guess"] if guesses else None,
-                   "restricted_rhs_at_zero": guesses[-1]["rhs_zero"] if guesses else None}
+                   "used_fraction": float(np.mean([g["used"] for g in guesses])) if guesses else None}
                   if net is not None else None),
         "solve": {"v_cycles": rep.get("iters"), "fp64_residuals": rep.get("fp64_residuals"),
                   "final_rel_resnorm_l2": (rep.get("final_resnorm_l2", 0) / rep["rhsnorm_l2"]) if rep else None,
