@@ -241,8 +241,11 @@ def test_learned_guess_rhs_without_eigenstrain(agb, oracle):
 @pytest.mark.gpu
 @pytest.mark.parametrize("where", ["host", "device"])
 def test_newton_solve_guess_one_call(agb, where):
-    """agb_newton_solve_guess equals agb_elastic_learned_guess followed by
-    agb_linear_solve (the same device work in one call)."""
+    """agb_newton_solve_guess does agb_elastic_learned_guess followed by
+    agb_linear_solve in one call.  A kept guess starts the single call's
+    mixed refinement from the FP32 residual of the fallback test (the two-call
+    form computes an FP64 one), so the two agree to the solve tolerance; a
+    dropped guess gives identical work."""
     from alamo_gb300 import learn
     n = 33
     C, F0, bc, dx = P.c1(n)
@@ -266,5 +269,9 @@ def test_newton_solve_guess_one_call(agb, where):
                                             tol_rel=1e-10, tol_abs=0.0)
             u1 = ut.cpu().numpy()
     assert r1["guess_used"] == used0
-    assert r1["iters"] == r0["iters"]
-    assert np.array_equal(u1, u0)
+    if used0:
+        assert abs(r1["iters"] - r0["iters"]) <= 2
+        assert np.abs(u1 - u0).max() <= 1e-7 * np.abs(u0).max()
+    else:
+        assert r1["iters"] == r0["iters"]
+        assert np.array_equal(u1, u0)
