@@ -275,3 +275,35 @@ def test_newton_solve_guess_one_call(agb, where):
     else:
         assert r1["iters"] == r0["iters"]
         assert np.array_equal(u1, u0)
+
+
+@pytest.mark.gpu
+def test_trained_guess_solve_matches_fp64(agb):
+    """The trained 65^3 network on a training-distribution medium at 65^3:
+    the single-call mixed solve from its guess (kept: the refinement starts
+    from the FP32 residual; dropped: from zero) reaches the plain FP64
+    solve's displacement."""
+    import os
+    from alamo_gb300 import learn
+    w = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "alamo_gb300", "weights",
+                     "unet65.npy")
+    if not os.path.exists(w):
+        pytest.skip("trained weights not present")
+    n = 65
+    C, F0, dx = learn.inclusion_medium(n, np.random.default_rng(2024))
+    bc = agb.bc.Constant()
+    opts = agb.default_opts(precision="mixed", solver="fgmres", bottom_solver="direct", max_coarsening_level=4,
+                            pre_smooth=1, post_smooth=1)
+    with learn.UNet(n) as net, agb.Elastic(n, dx, "isotropic", opts) as op:
+        net.load(w)
+        op.SetModel(np.ascontiguousarray(C))
+        op.SetBC(bc)
+        b = op.bc_init()
+        u = np.zeros((3, n, n, n))
+        r = agb.Newton(op).solve_guess(net, u, b, F0, tol_rel=1e-10, tol_abs=0.0)
+        op.SetOpts(agb.default_opts(precision="fp64"))
+        u64 = np.zeros((3, n, n, n))
+        agb.Newton(op).solve(u64, b, F0, tol_rel=1e-10, tol_abs=0.0)
+    assert r["status"] == 0
+    assert np.abs(u - u64).max() <= 1e-7 * np.abs(u64).max()
+    assert r["fp64_residuals"] >= 1
