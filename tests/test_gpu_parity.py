@@ -315,6 +315,59 @@ def test_uniaxial_known_answer_gpu(agb):
     assert np.sum((sig - E * 0.1 / 16) ** 2) / (n * (E * 0.1 / 16) ** 2) < 1e-8
 
 
+def _eshelby_golden():
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "eshelby.json")) as f:
+        return json.load(f)
+
+
+def test_eshelby_known_answer_gpu(agb, oracle):
+    """The reference's Eshelby test (tests/Eshelby/test) through the C ABI:
+    the FP64 Newton solve of the diffuse-ellipsoid eigenstrain on 129^3 over
+    [-4, 4]^3 equals the oracle's (solution and stress) and meets the
+    reference test's tolerance 0.1 against the analytic curves."""
+    n, hw = 129, 4.0
+    C, F0, bc, dx = P.eshelby(n, hw)
+    u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
+    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_iter=100)
+    so, _, _ = oracle.stress_strain(C, F0, xo, dx)
+    with make_op(agb, C, bc, dx) as op:
+        u = u0.copy()
+        rep = agb.Newton(op).solve(u, op.bc_init(), F0, tol_rel=1e-10, tol_abs=0.0)
+        s = op.Stress(u, F0)
+    assert rep["status"] == 0
+    assert rel(u, xo) <= 1e-8
+    assert rel(s.reshape(so.shape), so) <= 1e-8
+    uerr, serr = P.eshelby_errors(_eshelby_golden(), u, [s[..., 0, 0], s[..., 1, 1], s[..., 2, 2]], hw, dx)
+    assert np.all(uerr < 0.1) and np.all(serr < 0.1), (uerr, serr)
+
+
+@pytest.mark.slow
+def test_eshelby_mixed_257(agb):
+    """The Eshelby test on the reference's own domain [-8, 8]^3 at 257^3
+    nodes (spacing 1/16) with the benchmark's solver: learned-guess-free
+    mixed FP32/FP64 FGMRES(V(1,1)) to 1e-8, direct 5^3 bottom.  Displacement
+    and normal stress along x = y = 0.25 within the reference test's 0.1 of
+    the analytic solution."""
+    n, hw = 257, 8.0
+    C, F0, bc, dx = P.eshelby(n, hw)
+    nlev = 1
+    m = n
+    while (m - 1) % 2 == 0 and (m - 1) // 2 >= 2:
+        m = (m - 1) // 2 + 1
+        nlev += 1
+    with make_op(agb, C, bc, dx, precision="mixed", solver="fgmres", bottom_solver="direct",
+                 max_coarsening_level=nlev - 2, pre_smooth=1, post_smooth=1) as op:
+        del C
+        u = np.zeros((3, n, n, n))
+        rep = agb.Newton(op).solve(u, op.bc_init(), F0, tol_rel=1e-8, tol_abs=0.0)
+        s = op.Stress(u, F0)
+    assert rep["status"] == 0 and rep["final_resnorm"] <= 1e-8 * rep["rhsnorm0"]
+    uerr, serr = P.eshelby_errors(_eshelby_golden(), u, [s[..., 0, 0], s[..., 1, 1], s[..., 2, 2]], hw, dx)
+    assert np.all(uerr < 0.1) and np.all(serr < 0.1), (uerr, serr)
+
+
 # ------------------------------------------------------------ edge cases
 def test_non_cubic_grid(agb, oracle):
     C, _ = P.voronoi_clamp(33)[0], None

@@ -6,7 +6,10 @@
   cell tension test to the reference test's tolerance 1e-4 (fixture
   tests/golden/solid_trac_xhi.json, made by tests/golden/make_golden.py);
 - src/Test/Numeric/Stencil.H:58-106: derivative accuracy below 1e-2 on
-  cos(pi x/L) cos(pi y/L) cos(pi z/L) with 32 cells.
+  cos(pi x/L) cos(pi y/L) cos(pi z/L) with 32 cells;
+- tests/Eshelby/reference/Eshelby_{displacement,sigma_normal}.csv: the
+  analytic Eshelby inclusion solution along x = y = 0.25 to the reference
+  test's tolerance 0.1 (fixture tests/golden/eshelby.json).
 """
 import json
 import os
@@ -119,3 +122,32 @@ def test_stencil_accuracy(oracle, which):
     d = oracle.derivative(which, f, dx)
     s = (slice(1, -1),) * 3
     assert np.abs(d[s] - exact[s]).max() / np.abs(exact[s]).max() < 1e-2
+
+
+def test_eshelby_known_answer(oracle):
+    """The reference's Eshelby test (tests/Eshelby/test): eigenstrain 0.001 I
+    in a diffuse ellipsoid, zero displacement far away; displacement (relative
+    L2) and normal stress (relative L1) along x = y = 0.25 within 0.1 of the
+    analytic solution.  The reference runs [-8, 8]^3 with AMR down to a
+    spacing of 1/32 near the inclusion; here a uniform 129^3 grid over
+    [-4, 4]^3 (spacing 1/16).  Measured errors: u 0.017 / 0.019 / 0.029,
+    sigma 0.076 / 0.069 / 0.084 (sigma_zz is set by the resolution of the
+    0.5-wide z semi-axis, sigma_xx and sigma_yy by the clamped faces)."""
+    import problems as P
+    with open(os.path.join(GOLDEN, "eshelby.json")) as f:
+        golden = json.load(f)
+    n, hw = 129, 4.0
+    C, F0, bc, dx = P.eshelby(n, hw)
+    bt, bv = bc.tables()
+    u0 = np.zeros((3, n, n, n))
+    b = oracle.bc_init(np.zeros_like(u0), bt, bv)
+    rhs = oracle.build_rhs(C, F0, bt, u0, b, dx)
+    u, rep, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_iter=100)
+    assert rep.status == 0
+    s, _, _ = oracle.stress_strain(C, F0, u, dx)
+    uerr, serr = P.eshelby_errors(golden, u, [s[..., 0], s[..., 4], s[..., 8]], hw, dx)
+    assert np.all(uerr < 0.1), uerr
+    assert np.all(serr < 0.1), serr
+    # the solution is not trivially small: the inclusion's z displacement
+    # reaches 0.8 of its analytic peak on the ray
+    assert np.abs(u[2]).max() > 0.8 * np.abs(np.array(golden["displacement"]["disp3"])).max() / 1e4
