@@ -125,6 +125,9 @@ class Elastic:
         return out
 
     def SetBC(self, bc):
+        """Elastic::SetBC (src/Operator/Elastic.H:61-65).  The tables are
+        copied with the values at the BC's current time (``bc.set_time``);
+        after moving the time, call SetBC again."""
         self.bc = bc
         t, v = bc.tables()
         L.check(L.lib().agb_elastic_set_bc(self.h, t.ctypes.data_as(ctypes.c_void_p),

@@ -84,9 +84,12 @@ def test_solid_tension_series(oracle, name, f0):
     F0 = None if f0 is None else np.full((n, n, n), f0)
     u = np.zeros((3, n, n, n))
     times, trac = [], []
+    # the reference input: bc.tensiontest.type = uniaxial_stress,
+    # bc.tensiontest.disp = (0,1:0,0.01) (tests/Solid/input)
+    bc = B.TensionTest("uniaxial_stress", disp="(0,1:0,0.01)")
     for step in range(100):
         t = 0.01 * step
-        bt, bv = B.TensionTest("uniaxial_stress", disp=0.01 * t).tables()
+        bt, bv = bc.tables(t)
         b = oracle.bc_init(np.zeros_like(u), bt, bv)
         rhs = oracle.build_rhs(C, F0, bt, u, b, dx)
         du, rep, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-8, tol_abs=1e-8, max_iter=30)
