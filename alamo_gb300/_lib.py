@@ -61,6 +61,7 @@ class SolverOpts(ctypes.Structure):
         ("fine_kernel", ctypes.c_int),
         ("krylov_reorth", ctypes.c_int),
         ("tma_min_nodes", ctypes.c_int),
+        ("max_fmg_iter", ctypes.c_int),
     ]
 
 

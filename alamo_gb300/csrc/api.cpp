@@ -74,6 +74,9 @@ struct Lev {
     T* psi = nullptr;
     // 1 / diag of FP32 levels swept by the TMA kernels (their Jacobi form)
     T* dinv = nullptr;
+    // the F-cycle's interpolated start correction, kept while the V-cycle
+    // from this level runs (allocated by the first F-cycle)
+    T* hold = nullptr;
 };
 
 // Krylov space of the flexible GMRES: Arnoldi basis V (m+1 vectors), the
@@ -218,6 +221,7 @@ void free_levels(std::vector<Lev<T>>& L) {
         cudaFree(l.Cpad);
         cudaFree(l.psi);
         cudaFree(l.dinv);
+        cudaFree(l.hold);
     }
     L.clear();
 }
@@ -591,17 +595,18 @@ agb_status bottom<float>(agb_elastic* h, std::vector<Lev<float>>& L) {
     return AGB_OK;
 }
 
-// One V-cycle on the correction equation A cor = res of level 0
-// (MLMG::mgVcycle as driven by the reference's hooks).
+// One V-cycle on the correction equation A cor = res of level l0
+// (MLMG::mgVcycle(amrlev, mglev) as driven by the reference's hooks).
 template <typename T>
-agb_status vcycle(agb_elastic* h, std::vector<Lev<T>>& L) {
+agb_status vcycle(agb_elastic* h, std::vector<Lev<T>>& L, int l0 = 0) {
     const int nl = (int)L.size();
-    // levels above the bottom receive their first pre-smoothing sweep (from
-    // a zero correction) from the restriction that fills their right-hand side
+    if (l0 == nl - 1) return bottom<T>(h, L);
+    // levels below l0 receive their first pre-smoothing sweep (from a zero
+    // correction) from the restriction that fills their right-hand side
     const bool fuse = h->opts.pre_smooth > 0;
-    for (int l = 0; l < nl - 1; l++) {
+    for (int l = l0; l < nl - 1; l++) {
         Lev<T>& v = L[l];
-        TRY(smooth<T>(h, L, l, h->opts.pre_smooth, true, fuse && l > 0));
+        TRY(smooth<T>(h, L, l, h->opts.pre_smooth, true, fuse && l > l0));
         {
             ProfScope ps(h, Fam<T>::R, l == 0);
             if (use_zm<T>(h, v, l))
@@ -620,13 +625,55 @@ agb_status vcycle(agb_elastic* h, std::vector<Lev<T>>& L) {
         h->launches += 2;
     }
     TRY(bottom<T>(h, L));
-    for (int l = nl - 2; l >= 0; l--) {
+    for (int l = nl - 2; l >= l0; l--) {
         {
             ProfScope ps(h, AGB_K_PROLONG, l == 0);
             CK(launch_prolong_add<T>(L[l + 1].cor, L[l + 1].G, L[l].cor, L[l].G, h->stream));
         }
         h->launches++;
         TRY(smooth<T>(h, L, l, h->opts.post_smooth, false));
+    }
+    return AGB_OK;
+}
+
+// One F-cycle on A cor = res of the FP64 fine level, as MLMG::mgFcycle runs
+// it for the iterations below max_fmg_iter: the residual restricted to
+// every level, the bottom solve, then on each finer level the interpolated
+// coarse correction as a start (interpAssign: prolongation into a zeroed
+// correction), the residual of that start as the right-hand side of a
+// V-cycle from this level, and the start added back.
+agb_status fcycle64(agb_elastic* h) {
+    std::vector<Lev<double>>& L = h->L64;
+    const int nl = (int)L.size();
+    for (int l = 1; l < nl; l++) {
+        {
+            ProfScope ps(h, AGB_K_RESTRICT, l == 1);
+            CK(launch_restrict<double>(L[l - 1].res, L[l - 1].G, L[l].res, L[l].G, h->stream));
+        }
+        h->launches++;
+    }
+    TRY(bottom<double>(h, L));
+    for (int l = nl - 2; l >= 0; l--) {
+        Lev<double>& v = L[l];
+        Lev<double>& c = L[l + 1];
+        const int64_t n3 = 3 * v.G.N;
+        if (!v.hold) CK(cudaMalloc(&v.hold, sizeof(double) * n3));
+        CK(cudaMemsetAsync(v.cor, 0, sizeof(double) * n3, h->stream));
+        {
+            ProfScope ps(h, AGB_K_PROLONG, l == 0);
+            CK(launch_prolong_add<double>(c.cor, c.G, v.cor, v.G, h->stream));
+        }
+        {
+            ProfScope ps(h, AGB_K_RESIDUAL_F64, l == 0);
+            CK(launch_residual<double>(h->sym, v.cor, v.res, v.C, v.G, h->bc, v.rescor, nullptr, nullptr, h->stream));
+        }
+        h->launches += 2;
+        // res <- res - A start; keep the start; V-cycle; add the start back
+        std::swap(v.res, v.rescor);
+        std::swap(v.cor, v.hold);
+        TRY(vcycle<double>(h, L, l));
+        CK(launch_axpy(1.0, v.hold, v.cor, n3, h->stream));
+        h->launches++;
     }
     return AGB_OK;
 }
@@ -880,7 +927,8 @@ agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_re
                 h->launches++;
                 it += std::max(its, 1);
             } else if (!mixed) {
-                TRY(vcycle<double>(h, h->L64));
+                if (it < h->opts.max_fmg_iter) TRY(fcycle64(h));
+                else TRY(vcycle<double>(h, h->L64));
                 CK(launch_axpy(1.0, top.cor, x, n3, h->stream));
                 h->launches++;
                 it++;
@@ -1004,6 +1052,7 @@ agb_status agb_default_opts(agb_solver_opts* o) {
     o->fine_kernel = 0;
     o->krylov_reorth = 0;
     o->tma_min_nodes = 0;
+    o->max_fmg_iter = 100000000;
     return AGB_OK;
 }
 

@@ -308,6 +308,58 @@ class Elastic:
         return n.value
 
 
+# solver.* keys of Solver::Nonlocal::Linear::Parse (src/Solver/Nonlocal/Linear.H:296-382)
+# that map one to one onto agb_solver_opts fields
+_INT_KEYS = ["max_iter", "bottom_max_iter", "max_fmg_iter", "fixed_iter", "verbose", "pre_smooth", "post_smooth",
+             "final_smooth", "bottom_smooth"]
+_FLOAT_KEYS = ["bottom_tol_rel", "bottom_tol_abs", "omega"]
+# keys with no effect on a single-level solve: average_down_coeffs averages
+# stiffness between AMR levels only (Elastic.cpp:611-613); normalize_ddw is
+# stored but read by no operator code; dump_on_fail writes diagnostics files
+_NO_EFFECT_KEYS = ["average_down_coeffs", "normalize_ddw", "dump_on_fail"]
+
+
+def _flag(v):
+    if isinstance(v, str):
+        return v.strip().lower() in ("1", "true")
+    return bool(v)
+
+
+def parse_solver_opts(kv, opts=None):
+    """``Linear::Parse`` (src/Solver/Nonlocal/Linear.H:296-382) and
+    ``PrepareMLMG`` (:255-290): the reference's ``solver.*`` keys (given
+    without the prefix) onto an agb_solver_opts, starting from ``opts`` or
+    the defaults.  Returns (opts, extra) with extra = {"tol_rel", "tol_abs",
+    "abort_on_fail"} for the keys that are arguments of the solve.  The
+    deprecated keys abort in the reference and raise ValueError here, as do
+    unknown keys and the CG bottom solver (not provided: BiCGStab, the direct
+    bottom and the smoother are)."""
+    o = default_opts() if opts is None else opts
+    extra = {"tol_rel": None, "tol_abs": None, "abort_on_fail": True}
+    for k, v in kv.items():
+        if k in ("max_fixed_iter", "cg_tol_rel", "cg_tol_abs"):
+            raise ValueError(k + " is deprecated in the reference (Linear.H:308-335)")
+        if k in _INT_KEYS:
+            setattr(o, k, int(v))
+        elif k in _FLOAT_KEYS:
+            setattr(o, k, float(v))
+        elif k == "bottom_solver":
+            name = str(v).strip()
+            if name == "cg":
+                raise ValueError("the CG bottom solver is not provided (bicgstab, direct, smoother are)")
+            o.bottom_solver = {"bicgstab": L.BOTTOM_BICGSTAB, "direct": L.BOTTOM_DIRECT,
+                               "smoother": L.BOTTOM_SMOOTHER}[name]
+        elif k in ("tol_rel", "tol_abs"):
+            extra[k] = float(v)
+        elif k == "abort_on_fail":
+            extra["abort_on_fail"] = _flag(v)
+        elif k in _NO_EFFECT_KEYS:
+            pass
+        else:
+            raise KeyError("unknown solver key " + k)
+    return o, extra
+
+
 class Linear:
     """Solver::Nonlocal::Linear: multigrid solve of A sol = rhs."""
 
@@ -330,7 +382,22 @@ class Linear:
             setattr(o, k, v)
         self.op.SetOpts(o)
 
+    def Parse(self, kv):
+        """Apply the reference's ``solver.*`` keys (parse_solver_opts) to the
+        operator's options; tol_rel / tol_abs / abort_on_fail are kept on
+        the solver for the caller."""
+        o, extra = parse_solver_opts(kv, self.op.opts)
+        self.op.SetOpts(o)
+        self.parsed = extra
+        return extra
+
+    def apply(self, rhs, sol):
+        """Linear::apply (src/Solver/Nonlocal/Linear.H:169-174): rhs = A sol
+        on the fine level, boundary rows included."""
+        return self.op.Fapply(sol, rhs)
+
     def setMaxIter(self, v): self._set(max_iter=int(v))
+    def setMaxFmgIter(self, v): self._set(max_fmg_iter=int(v))
     def setBottomMaxIter(self, v): self._set(bottom_max_iter=int(v))
     def setFixedIter(self, v): self._set(fixed_iter=int(v))
     def setVerbose(self, v): self._set(verbose=int(v))

@@ -96,6 +96,10 @@ typedef struct agb_solver_opts {
     int krylov_reorth;        /* FGMRES Gram-Schmidt: 1 re-orthogonalise once, 0 single pass (default) */
     int tma_min_nodes;        /* FP32 levels with at least this many nodes use the z-marching kernels
                                  (fine_kernel 0); smaller ones the per-node kernels (0: 30000) */
+    int max_fmg_iter;         /* FP64 multigrid iteration (solver AGB_SOLVER_VCYCLE, precision FP64):
+                                 iterations below this count run an F-cycle (MLMG::mgFcycle), later
+                                 ones a V-cycle; Linear::PrepareMLMG sets 100000000, so every
+                                 iteration is an F-cycle (src/Solver/Nonlocal/Linear.H:261) (100000000) */
 } agb_solver_opts;
 
 typedef struct agb_solve_report {

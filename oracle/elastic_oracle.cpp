@@ -632,6 +632,8 @@ struct orc_opts {
     int fixed_iter;            // -1 = run to tolerance
     int verbose;
     int bottom_solver;         // 0 BiCGStab, 1 dense direct (exact), 2 smoother only
+    int max_fmg_iter;          // iterations that run an F-cycle before V-cycles take over
+                               // (Linear::PrepareMLMG sets 100000000, Linear.H:261)
 };
 
 struct orc_report {
@@ -953,7 +955,7 @@ namespace {
 
 struct Level {
     Grid g;
-    std::vector<double> C, diag, res, cor, rescor, tmp, psi;
+    std::vector<double> C, diag, res, cor, rescor, tmp, psi, hold;
 };
 
 // psi of level l > 0 coarsened from level l - 1 (prepareForSolve order:
@@ -1109,9 +1111,11 @@ struct Hier {
         }
     }
 
-    void vcycle() {
+    // V-cycle on A cor = res of level l0 (MLMG::mgVcycle(amrlev, mglev))
+    void vcycle(int l0 = 0) {
         const int nl = (int)L.size();
-        for (int l = 0; l < nl - 1; l++) {
+        if (l0 == nl - 1) { bottom(); return; }
+        for (int l = l0; l < nl - 1; l++) {
             Level& v = L[l];
             std::fill(v.cor.begin(), v.cor.end(), 0.0);
             smooth(l, o.pre_smooth);
@@ -1121,12 +1125,45 @@ struct Hier {
             restrict_generic(v.g, c.g, v.rescor.data(), c.res.data(), 3, v.g.N(), 1, c.g.N(), 1);
         }
         bottom();
-        for (int l = nl - 2; l >= 0; l--) {
+        for (int l = nl - 2; l >= l0; l--) {
             Level& v = L[l];
             Level& c = L[l + 1];
             prolong_add(v.g, c.g, c.cor.data(), v.cor.data(), 3);
             smooth(l, o.post_smooth);
         }
+    }
+
+    // F-cycle on A cor = res of level 0, as MLMG::mgFcycle runs it for the
+    // iterations below max_fmg_iter: the residual restricted to every level,
+    // the bottom solve, then on each finer level the interpolated coarse
+    // correction as a start (interpAssign), the residual of that correction
+    // as the right-hand side of a V-cycle from this level, and the
+    // interpolated start added back.  The residual goes down with the
+    // operator's restriction (Operator.cpp:262-363), the correction up with
+    // its interpolation (:365-434) into a zeroed fine correction.
+    void fcycle() {
+        const int nl = (int)L.size();
+        for (int l = 1; l < nl; l++)
+            restrict_generic(L[l - 1].g, L[l].g, L[l - 1].res.data(), L[l].res.data(), 3, L[l - 1].g.N(), 1,
+                             L[l].g.N(), 1);
+        bottom();
+        for (int l = nl - 2; l >= 0; l--) {
+            Level& v = L[l];
+            Level& c = L[l + 1];
+            std::fill(v.cor.begin(), v.cor.end(), 0.0);
+            prolong_add(v.g, c.g, c.cor.data(), v.cor.data(), 3);
+            residual(sym, v.g, v.C.data(), bct, v.cor.data(), v.res.data(), v.rescor.data());
+            std::swap(v.res, v.rescor);
+            v.hold.swap(v.cor);
+            v.cor.assign(v.hold.size(), 0.0);
+            vcycle(l);
+            for (size_t q = 0; q < v.cor.size(); q++) v.cor[q] += v.hold[q];
+        }
+    }
+
+    void cycle(int iter) {
+        if (iter < o.max_fmg_iter) fcycle();
+        else vcycle();
     }
 };
 
@@ -1146,6 +1183,7 @@ void orc_default_opts(orc_opts* o) {
     o->fixed_iter = -1;
     o->verbose = 0;
     o->bottom_solver = 0;
+    o->max_fmg_iter = 100000000;
 }
 
 // number of multigrid levels for a node grid (coarsen by 2 while every
@@ -1254,7 +1292,7 @@ int orc_solve(int sym, int nx, int ny, int nz, const double* dx, const double* C
     if (rn <= target && opts->fixed_iter <= 0) status = 0;
     else {
         for (it = 0; it < maxit; it++) {
-            H.vcycle();
+            H.cycle(it);
             for (int64_t q = 0; q < n3; q++) sol[q] += top.cor[q];
             rn = residual(sym, top.g, top.C.data(), bc_type, sol, rhs, top.res.data());
             if (res_hist) res_hist[it + 1] = rn;

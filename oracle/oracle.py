@@ -37,6 +37,7 @@ class Opts(ctypes.Structure):
         ("fixed_iter", ctypes.c_int),
         ("verbose", ctypes.c_int),
         ("bottom_solver", ctypes.c_int),
+        ("max_fmg_iter", ctypes.c_int),
     ]
 
 

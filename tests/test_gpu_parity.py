@@ -143,32 +143,68 @@ def newton_problem(agb, oracle, C, F0, bc, dx):
     return u0, b, rhs, bt
 
 
+FMG = {"V": 0, "F": 100000000}
+
+
+@pytest.mark.parametrize("cycle", ["V", "F"])
 @pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
-def test_vcycle_iterates_match(agb, oracle, case):
-    """Three V-cycles from zero: the GPU iterate equals the oracle's."""
+def test_vcycle_iterates_match(agb, oracle, case, cycle):
+    """Three multigrid iterations from zero, V-cycles (max_fmg_iter 0) or
+    the F-cycles the reference runs by default: the GPU iterate equals the
+    oracle's.  The F-cycle calls the bottom solve once per level, so it runs
+    with the exact dense bottom (BiCGStab's relative stopping test moves its
+    output at the 1e-6 level under rounding-level input changes)."""
     C, F0, bc, dx = CASES[case]()
     u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
-    xo, rep_o, hist_o = oracle.solve(C, bt, rhs, dx, fixed_iter=3)
-    with make_op(agb, C, bc, dx, fixed_iter=3) as op:
+    kw = {"max_fmg_iter": FMG[cycle]}
+    if cycle == "F":
+        kw.update(bottom_solver=1, max_coarsening_level=oracle.num_levels(*C.shape[:3]) - 2)
+    xo, rep_o, hist_o = oracle.solve(C, bt, rhs, dx, fixed_iter=3, **kw)
+    with make_op(agb, C, bc, dx, fixed_iter=3, **kw) as op:
         x = u0.copy()
         rep = agb.Linear(op).solve(x, rhs, 1e-30, 0.0)
     assert rep["iters"] == 3
     assert rel(x, xo) <= 1e-10
 
 
-@pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
-def test_solve_parity(agb, oracle, case):
-    """Config 1 runs V(2,2) cycles to 1e-10: same cycle count, same solution."""
+@pytest.mark.parametrize("case,cycle", [("c1-iso", "V"), ("voronoi-mm", "V"), ("voronoi-mm", "F")])
+def test_solve_parity(agb, oracle, case, cycle):
+    """Solves to 1e-10: same cycle count, same solution.  Config 1 runs
+    V(2,2) V-cycles: the reference's default F-cycles stall near 7e-9 on it
+    (test_reference_vcycle_instability)."""
     C, F0, bc, dx = CASES[case]()
     u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
-    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10)
+    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_fmg_iter=FMG[cycle])
     assert rep_o.status == 0
-    with make_op(agb, C, bc, dx) as op:
+    with make_op(agb, C, bc, dx, max_fmg_iter=FMG[cycle]) as op:
         u = u0.copy()
         rep = agb.Newton(op).solve(u, b, F0, tol_rel=1e-10, tol_abs=0.0)
     assert rep["status"] == 0 and abs(rep["iters"] - rep_o.iters) <= 1
     assert rep["final_resnorm"] <= 1e-10 * rep["rhsnorm0"]
     assert rel(u, xo) <= 1e-8
+
+
+def test_fcycle_solve_matches_oracle_spheres(agb, oracle):
+    """The reference's default iteration (F-cycles, BiCGStab bottom), set
+    through Linear.Parse with the reference's solver keys, on a diffuse-sphere
+    medium: the oracle's cycle count (17 to 1e-10 at 33^3; V-cycles take 26) and
+    solution; Linear.apply gives back the right-hand side."""
+    from alamo_gb300 import synth, bc as B
+    n = 33
+    C, F0, dx, _ = synth.spheres_diffuse(n, 30, seed=3, rmin=0.05, rmax=0.12)
+    bc = B.Constant()
+    u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
+    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10)
+    assert rep_o.status == 0
+    with make_op(agb, C, bc, dx, max_fmg_iter=0) as op:
+        solver = agb.Linear(op)
+        extra = solver.Parse({"max_fmg_iter": 100000000, "tol_rel": 1e-10, "tol_abs": 0})
+        x = u0.copy()
+        rep = solver.solve(x, rhs, extra["tol_rel"], extra["tol_abs"])
+        f = solver.apply(np.empty_like(x), x)
+    assert rep["status"] == 0 and abs(rep["iters"] - rep_o.iters) <= 1
+    assert rel(x, xo) <= 1e-8
+    assert rel(f, rhs) <= 1e-9
 
 
 @pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm", "mm-randbc"])
@@ -243,7 +279,7 @@ def test_mixed_precision_solve(agb, oracle, case):
     FP32 rounding excites, so config 1 runs the FGMRES(V-cycle) form."""
     C, F0, bc, dx = CASES[case]()
     u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
-    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10)
+    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_fmg_iter=0)
     solver = 1 if case == "c1-iso" else 0
     with make_op(agb, C, bc, dx, precision=1, solver=solver) as op:
         u = u0.copy()
@@ -261,7 +297,8 @@ def test_fgmres_solve(agb, oracle, case, prec):
     refinement) reaches the same solution as the oracle's V-cycle solve."""
     C, F0, bc, dx = CASES[case]()
     u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
-    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10)
+    # against the V-cycle iteration (max_fmg_iter 0), which FGMRES wraps
+    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_fmg_iter=0)
     with make_op(agb, C, bc, dx, solver=1, precision=prec, bottom_solver=1,
                  max_coarsening_level=oracle.num_levels(*C.shape[:3]) - 2) as op:
         u = u0.copy()
@@ -288,7 +325,7 @@ def test_fgmres_where_vcycle_diverges(agb, oracle):
         e[q] = 1.0
         M[:, q] = oracle.fapply(C, bt, e.reshape(3, n, n, n), dx).ravel()
     xd = np.linalg.solve(M, rhs.ravel()).reshape(rhs.shape)
-    _, rep_v, hist = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_iter=60)
+    _, rep_v, hist = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_iter=60, max_fmg_iter=0)
     assert rep_v.status != 0 and hist[-1] > hist[0]  # the V-cycle iteration diverges here
     for prec in (0, 1):
         with make_op(agb, C, bc, dx, solver=1, precision=prec) as op:

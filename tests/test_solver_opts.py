@@ -1,0 +1,36 @@
+"""Host-side solver settings (no GPU): the reference's solver.* keys onto the
+C ABI's agb_solver_opts, and the defaults Linear::PrepareMLMG gives MLMG."""
+import pytest
+
+
+def test_default_cycle_is_the_reference_f_cycle(agb):
+    """Linear::PrepareMLMG calls setMaxFmgIter(100000000) and Parse leaves
+    it unless solver.max_fmg_iter is given (Linear.H:261-266)."""
+    assert agb.default_opts().max_fmg_iter == 100000000
+
+
+def test_parse_maps_reference_keys(agb):
+    from alamo_gb300 import _lib
+    from alamo_gb300.elastic import parse_solver_opts
+    o, extra = parse_solver_opts({
+        "max_iter": "500", "bottom_max_iter": 50, "max_fmg_iter": "0", "fixed_iter": 4, "verbose": 3,
+        "pre_smooth": 1, "post_smooth": "3", "final_smooth": 6, "bottom_smooth": 2, "bottom_solver": "smoother",
+        "bottom_tol_rel": "1e-6", "bottom_tol_abs": 1e-12, "omega": 0.5, "tol_rel": "1e-9", "tol_abs": 0,
+        "average_down_coeffs": "true", "normalize_ddw": 1, "abort_on_fail": "false"})
+    assert (o.max_iter, o.bottom_max_iter, o.max_fmg_iter, o.fixed_iter, o.verbose) == (500, 50, 0, 4, 3)
+    assert (o.pre_smooth, o.post_smooth, o.final_smooth, o.bottom_smooth) == (1, 3, 6, 2)
+    assert o.bottom_solver == _lib.BOTTOM_SMOOTHER
+    assert (o.bottom_tol_rel, o.bottom_tol_abs, o.omega) == (1e-6, 1e-12, 0.5)
+    assert extra == {"tol_rel": 1e-9, "tol_abs": 0.0, "abort_on_fail": False}
+    # untouched fields keep the defaults they started from
+    d = agb.default_opts()
+    assert (o.precision, o.solver, o.krylov_dim) == (d.precision, d.solver, d.krylov_dim)
+
+
+@pytest.mark.parametrize("kv,err", [({"max_fixed_iter": 3}, ValueError), ({"cg_tol_rel": 1e-3}, ValueError),
+                                    ({"cg_tol_abs": 1e-3}, ValueError), ({"bottom_solver": "cg"}, ValueError),
+                                    ({"bottom_solver": "jacobi"}, KeyError), ({"max_iters": 3}, KeyError)])
+def test_parse_rejects(agb, kv, err):
+    from alamo_gb300.elastic import parse_solver_opts
+    with pytest.raises(err):
+        parse_solver_opts(kv)
