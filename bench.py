@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 # 100000000 (the oracle and the GPU FP64 path iterate identically); used to
 # scale the CPU sample to a whole solve when the run has no plain FP64 solve
 # of its own to count them.
-FP64_CYCLES = {"c1": 18, "c2": 50, "c3": 26}
+FP64_CYCLES = {"c1": 18, "c2": 50, "c3": 16}
 
 # bytes each kernel family must move per fine-level node (each array once)
 BYTES_PER_NODE = {
