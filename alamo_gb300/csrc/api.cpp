@@ -1,5 +1,5 @@
 // Host driver of alamo_gb300: the C ABI of include/agb.h, the multigrid
-// hierarchy, the V-cycle and the solves.
+// hierarchy, the multigrid cycles and the solves.
 //
 // Mapping to the reference (Gopal-B/alamo):
 //   agb_elastic            Operator::Elastic<SYM> + Solver::Nonlocal::Linear
@@ -9,6 +9,8 @@
 //   vcycle<T>()            the MLMG V-cycle that calls the operator's hooks
 //                          (Fsmooth, correctionResidual, restriction,
 //                          interpolation, bottom BiCGStab)
+//   fcycle64()             the MLMG F-cycle (max_fmg_iter iterations; the
+//                          reference sets 100000000, Linear.H:261)
 //   solve_fp64 / mixed     Linear::solve (src/Solver/Nonlocal/Linear.H:131)
 //   agb_newton_solve       Newton::solve, nriters = 1
 //                          (src/Solver/Nonlocal/Newton.H:279-358)

@@ -57,8 +57,10 @@ typedef enum {
     AGB_BC_NONE = 4
 } agb_bc_type;
 typedef enum { AGB_PRECISION_FP64 = 0, AGB_PRECISION_MIXED = 1 } agb_precision;
-/* AGB_SOLVER_VCYCLE: V-cycles on the correction equation as amrex::MLMG runs
- * them for the reference.  AGB_SOLVER_FGMRES: flexible GMRES whose
+/* AGB_SOLVER_VCYCLE: multigrid iterations on the correction equation as
+ * amrex::MLMG runs them for the reference (F-cycles while the iteration count
+ * is below opts.max_fmg_iter, V-cycles after; FP32 V-cycles in mixed
+ * precision).  AGB_SOLVER_FGMRES: flexible GMRES whose
  * preconditioner is one V-cycle (AMReX's GMRES-with-MLMG-preconditioner
  * scheme); in mixed precision the FGMRES and its V-cycle run in FP32 inside
  * FP64 iterative refinement.  Both stop on the same FP64 residual test. */
@@ -73,7 +75,7 @@ typedef enum { AGB_BOTTOM_BICGSTAB = 0, AGB_BOTTOM_DIRECT = 1, AGB_BOTTOM_SMOOTH
 /* Solver settings; field names follow the reference's `solver.*` keys
  * (Solver::Nonlocal::Linear::Parse, src/Solver/Nonlocal/Linear.H:296-382). */
 typedef struct agb_solver_opts {
-    int max_iter;             /* V-cycles before AGB_NOT_CONVERGED (200) */
+    int max_iter;             /* multigrid iterations before AGB_NOT_CONVERGED (200) */
     int pre_smooth;           /* Fsmooth calls before restriction (2) */
     int post_smooth;          /* Fsmooth calls after prolongation (2) */
     int final_smooth;         /* Fsmooth calls after a failed bottom solve (8) */
@@ -104,7 +106,8 @@ typedef struct agb_solver_opts {
 
 typedef struct agb_solve_report {
     int status;               /* agb_status of the solve */
-    int iters;                /* V-cycles (FP32 cycles in mixed precision) */
+    int iters;                /* multigrid iterations: F- or V-cycles in FP64, FP32 V-cycles in
+                                 mixed precision (FGMRES: preconditioner V-cycles) */
     int nlevels;
     int bottom_iters;         /* BiCGStab iterations summed over cycles (last read) */
     int fp64_residuals;       /* FP64 fine-level residual evaluations */
@@ -205,7 +208,8 @@ agb_status agb_elastic_bc_init(agb_elastic* h, double* b, int homogeneous, int w
 agb_status agb_elastic_build_rhs(agb_elastic* h, const double* u, const double* b, const double* F0, int f0_ncomp,
                                  double* rhs, int where);
 /* Solver::Nonlocal::Linear::solve (src/Solver/Nonlocal/Linear.H:131-147):
- * V-cycles on A sol = rhs from the initial guess in sol until
+ * multigrid iterations (opts.max_fmg_iter: F-cycles, then V-cycles) or
+ * FGMRES on A sol = rhs from the initial guess in sol until
  * ||rhs - A sol||_inf <= max(tol_abs, tol_rel * max(||rhs||_inf, ||r0||_inf)).
  * opts.precision selects the plain FP64 cycle or FP32 cycles inside FP64
  * iterative refinement.  rep may be NULL. */

@@ -40,8 +40,10 @@
 //                     src/Solver/Nonlocal/Linear.H:255-290 (AMReX itself is not
 //                     vendored in the reference: parity is unpinned at the MLMG
 //                     boundary, the loop below restates its published
-//                     behaviour: V-cycle on the correction equation, BiCGStab
-//                     bottom on the diagonally normalised system, inf-norm test)
+//                     behaviour: F-cycles (max_fmg_iter = 100000000,
+//                     Linear.H:261) or V-cycles on the correction equation,
+//                     BiCGStab bottom on the diagonally normalised system,
+//                     inf-norm test)
 //
 // Pinned against the reference's own known answers (tests/test_oracle_golden.py):
 //   tests/UniaxialTension (linear exactness, 1e-8), tests/Solid/reference/
@@ -619,7 +621,7 @@ double dot(const double* a, const double* b, int64_t n) {
 extern "C" {
 
 struct orc_opts {
-    int max_iter;              // MLMG max V-cycles (AMReX default 200)
+    int max_iter;              // MLMG max iterations (AMReX default 200)
     int pre_smooth;            // Fsmooth calls before restriction (2)
     int post_smooth;           // Fsmooth calls after prolongation (2)
     int final_smooth;          // Fsmooth calls when the bottom solve fails (8)
@@ -948,8 +950,9 @@ void orc_cubic(double C11, double C12, double C44, const double* R, double* out2
 
 // ---------------------------------------------------------------------------
 // Multigrid solve of A x = rhs on one AMR level, restating amrex::MLMG as
-// configured by Solver::Nonlocal::Linear (V-cycles on the correction
-// equation, BiCGStab bottom on the diagonally normalised system).
+// configured by Solver::Nonlocal::Linear (F-cycles, or V-cycles after
+// max_fmg_iter iterations, on the correction equation; BiCGStab bottom on the
+// diagonally normalised system).
 // ---------------------------------------------------------------------------
 namespace {
 
