@@ -1,7 +1,8 @@
 """Internal consistency of the oracle (CPU): the diagonal equals the operator
 probed with unit vectors, isotropic stiffness written as 21 major-minor
 entries gives the same operator, the transfer operators reproduce the
-fields they must, and the V-cycle converges on config 1."""
+fields they must, the multigrid iteration converges on config 1, and the
+F-cycle is MLMG's mgFcycle built from the oracle's own V-cycles."""
 import numpy as np
 import pytest
 
@@ -162,3 +163,32 @@ def test_reference_vcycle_diverges_on_sharp_spheres(oracle):
         hists[eps] = hist / hist[0]
     assert hists[0][-1] > 1e3
     assert hists[2][-1] < 1e-10
+
+
+@pytest.mark.parametrize("case", ["c1", "voronoi"])
+def test_fcycle_is_mgfcycle_composed_of_vcycles(oracle, case):
+    """The oracle's F-cycle equals MLMG::mgFcycle composed from the oracle's
+    own parts: residual restricted to every level, bottom solve on the
+    coarsest, then per finer level the interpolated coarse correction as a
+    start, one V-cycle from that level on the residual of the start (its own
+    hierarchy of the coarsened stiffness), and the start added back."""
+    C, F0, bc, dx = P.c1(17) if case == "c1" else P.voronoi_clamp(17)
+    if case == "voronoi":
+        bc = P.random_bc(5)  # keeps the 3^3 bottom regular for the dense solve
+    n = 17
+    bt, _ = bc.tables()
+    nl = oracle.num_levels(n, n, n)
+    res0 = P.random_field((3, n, n, n), 41)
+    Cs, dxs, res = [C], [dx], [res0]
+    for _ in range(1, nl):
+        Cs.append(oracle.restrict_C(Cs[-1]))
+        dxs.append(2 * dxs[-1])
+        res.append(oracle.restrict(res[-1]))
+    cor = oracle.vcycle(Cs[-1], bt, res[-1], dxs[-1], max_coarsening_level=0, bottom_solver=1)
+    for lev in range(nl - 2, -1, -1):
+        start = oracle.prolong_add(cor, np.zeros_like(res[lev]))
+        r, _ = oracle.residual(Cs[lev], bt, start, res[lev], dxs[lev])
+        cor = oracle.vcycle(Cs[lev], bt, r, dxs[lev], max_coarsening_level=nl - 1 - lev, bottom_solver=1) + start
+    x, rep, _ = oracle.solve(C, bt, res0, dx, fixed_iter=1, bottom_solver=1)
+    assert rep.nlevels == nl
+    assert np.abs(x - cor).max() <= 1e-12 * np.abs(cor).max()
