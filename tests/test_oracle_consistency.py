@@ -192,3 +192,32 @@ def test_fcycle_is_mgfcycle_composed_of_vcycles(oracle, case):
     x, rep, _ = oracle.solve(C, bt, res0, dx, fixed_iter=1, bottom_solver=1)
     assert rep.nlevels == nl
     assert np.abs(x - cor).max() <= 1e-12 * np.abs(cor).max()
+
+
+def test_vcycle_is_mgvcycle_composed_of_hooks(oracle):
+    """The oracle's V-cycle equals MLMG::mgVcycle composed from the operator
+    hooks: per level a zero correction, pre_smooth Fsmooth calls, the
+    correction residual restricted down; the bottom solve; prolongation added
+    and post_smooth Fsmooth calls on the way up."""
+    C, F0, _, dx = P.voronoi_clamp(17)
+    bt, _ = P.random_bc(5).tables()
+    n = 17
+    nl = oracle.num_levels(n, n, n)
+    res0 = P.random_field((3, n, n, n), 43)
+    Cs, dxs = [C], [dx]
+    for _ in range(1, nl):
+        Cs.append(oracle.restrict_C(Cs[-1]))
+        dxs.append(2 * dxs[-1])
+    dgs = [oracle.diagonal(c, bt, d) for c, d in zip(Cs, dxs)]
+
+    def cycle(lev, res):
+        if lev == nl - 1:
+            return oracle.vcycle(Cs[lev], bt, res, dxs[lev], max_coarsening_level=0, bottom_solver=1)
+        cor = oracle.fsmooth(Cs[lev], bt, dgs[lev], np.zeros_like(res), res, dxs[lev], ncalls=2)
+        r, _ = oracle.residual(Cs[lev], bt, cor, res, dxs[lev])
+        cor = oracle.prolong_add(cycle(lev + 1, oracle.restrict(r)), cor)
+        return oracle.fsmooth(Cs[lev], bt, dgs[lev], cor, res, dxs[lev], ncalls=2)
+
+    ref = cycle(0, res0)
+    out = oracle.vcycle(C, bt, res0, dx, bottom_solver=1)
+    assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
