@@ -192,9 +192,12 @@ def cpu_sample(cfg, n_override, C, F0, bc, dx, cycles):
     per_cycle = (rep.seconds - rep.setup_seconds) / sample_cycles
     setup = rep.setup_seconds + t_rhs
     est = setup + per_cycle * cycles
-    # one operator application at full size, median of three
+    # one V-cycle (max_fmg_iter 0) for comparison with the GPU's V-cycles
+    _, repv, _ = O.solve(C, bt, rhs, dx, fixed_iter=1, max_fmg_iter=0)
+    v_cycle = repv.seconds - repv.setup_seconds
+    # one operator application at full size, median of ten
     fap = []
-    for _ in range(3):
+    for _ in range(10):
         t3 = time.perf_counter()
         O.fapply(C, bt, x, dx)
         fap.append(time.perf_counter() - t3)
@@ -203,7 +206,7 @@ def cpu_sample(cfg, n_override, C, F0, bc, dx, cycles):
                       "set-up + %d fixed FP64 F-cycles at the full %d^3 size; solve time = set-up + "
                       "per-cycle time x %d cycles (the FP64 F-cycle count of this input to 1e-8)"
                       % (threads, sample_cycles, n, cycles),
-            "per_cycle_s": per_cycle, "setup_s": setup, "fapply_s": float(np.median(fap)),
+            "per_cycle_s": per_cycle, "v_cycle_s": v_cycle, "setup_s": setup, "fapply_s": float(np.median(fap)),
             "fapply_node_updates_per_s": float(n ** 3 / np.median(fap)), "sample_wall_s": time.perf_counter() - t0}
 
 
