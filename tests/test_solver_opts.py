@@ -34,3 +34,33 @@ def test_parse_rejects(agb, kv, err):
     from alamo_gb300.elastic import parse_solver_opts
     with pytest.raises(err):
         parse_solver_opts(kv)
+
+
+@pytest.mark.parametrize("field,value", [
+    ("pre_smooth", -1), ("post_smooth", -1), ("final_smooth", -1), ("bottom_smooth", -1),
+    ("bottom_max_iter", -1), ("max_iter", -1), ("omega", 0.0), ("omega", 2.5), ("precision", 5),
+    ("solver", 3), ("bottom_solver", 7), ("fine_kernel", 3), ("tma_min_nodes", -1)])
+def test_create_rejects_bad_options(agb, field, value):
+    """agb_elastic_create checks the options before it touches the GPU and
+    answers AGB_BAD_ARG with a message naming the problem."""
+    import ctypes
+    from alamo_gb300 import _lib
+    o = agb.default_opts()
+    setattr(o, field, value)
+    h = ctypes.c_void_p()
+    dx = (ctypes.c_double * 3)(1, 1, 1)
+    assert agb.lib().agb_elastic_create(ctypes.byref(h), 5, 5, 5, dx, 0, ctypes.byref(o)) == _lib.AGB_BAD_ARG
+    assert not h.value
+    assert _lib.last_error()
+
+
+@pytest.mark.parametrize("field,value", [("krylov_dim", 0), ("krylov_dim", 40), ("inner_tol", 0.0),
+                                         ("inner_tol", 1.0)])
+def test_create_rejects_bad_fgmres_options(agb, field, value):
+    import ctypes
+    from alamo_gb300 import _lib
+    o = agb.default_opts(solver="fgmres")
+    setattr(o, field, value)
+    h = ctypes.c_void_p()
+    dx = (ctypes.c_double * 3)(1, 1, 1)
+    assert agb.lib().agb_elastic_create(ctypes.byref(h), 5, 5, 5, dx, 0, ctypes.byref(o)) == _lib.AGB_BAD_ARG
