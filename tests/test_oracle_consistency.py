@@ -221,3 +221,34 @@ def test_vcycle_is_mgvcycle_composed_of_hooks(oracle):
     ref = cycle(0, res0)
     out = oracle.vcycle(C, bt, res0, dx, bottom_solver=1)
     assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("nc", [21, 45])
+def test_matrix4_symmetries(oracle, nc):
+    """Test::Set::Matrix4::SymmetryTest (src/Test/Set/Matrix4.H:46-97) through
+    the oracle's stress: a random MajorMinor tensor (21 values) has major and
+    both minor symmetries -- sigma(G) = sigma(G^T), sigma(G) symmetric,
+    sigma(G1):G2 = sigma(G2):G1 -- and a random Major tensor (45 values) the
+    major one.  The gradient G is imposed as the linear field u = G x."""
+    rng = np.random.default_rng(11)
+    n = 5
+    dx = 0.25
+    xs = dx * np.arange(n)
+    Z, Y, X = np.meshgrid(xs, xs, xs, indexing="ij")
+    C = np.empty((n, n, n, nc))
+    C[...] = rng.uniform(-1, 1, nc)
+
+    def sigma(G):
+        u = np.stack([G[i, 0] * X + G[i, 1] * Y + G[i, 2] * Z for i in range(3)])
+        s, _, _ = oracle.stress_strain(C, None, np.ascontiguousarray(u), dx)
+        return s[2, 2, 2].reshape(3, 3)
+
+    G1, G2 = rng.uniform(-1, 1, (3, 3)), rng.uniform(-1, 1, (3, 3))
+    s1, s2 = sigma(G1), sigma(G2)
+    assert abs(np.sum(s1 * G2) - np.sum(s2 * G1)) <= 1e-12 * np.abs(s1).max() * 9
+    if nc == 21:
+        assert np.allclose(s1, s1.T, rtol=0, atol=1e-13)
+        assert np.allclose(sigma(G1.T), s1, rtol=0, atol=1e-13)
+    else:
+        # Major alone: sigma depends on the whole gradient, not on its symmetric part
+        assert not np.allclose(sigma(G1.T), s1, rtol=0, atol=1e-6)
