@@ -225,7 +225,7 @@ def test_vcycle_is_mgvcycle_composed_of_hooks(oracle):
 
 @pytest.mark.parametrize("nc", [21, 45])
 def test_matrix4_symmetries(oracle, nc):
-    """Test::Set::Matrix4::SymmetryTest (src/Test/Set/Matrix4.H:46-97) through
+    """Test::Set::Matrix4::SymmetryTest (src/Test/Set/Matrix4.H:45-104) through
     the oracle's stress: a random MajorMinor tensor (21 values) has major and
     both minor symmetries -- sigma(G) = sigma(G^T), sigma(G) symmetric,
     sigma(G1):G2 = sigma(G2):G1 -- and a random Major tensor (45 values) the
