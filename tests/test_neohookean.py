@@ -76,6 +76,28 @@ def test_neohookean_ddw_is_the_gradient_of_dw(oracle):
                 q += 1
 
 
+def test_neohookean_material_frame_indifference(oracle):
+    """Model::Solid::Solid::MaterialFrameIndifference (src/Model/Solid/
+    Solid.H:210-262): W(R F) = W(F) for rotations R and det F in [0.5, 2],
+    relative to |W(RF) + W(F)| + 1e-4, tolerance 1e-4 (here far below it)."""
+    rng = np.random.default_rng(3)
+    for _ in range(10):
+        F = rng.uniform(-1, 1, (3, 3))
+        while not 0.5 <= np.linalg.det(F) <= 2.0:
+            F = rng.uniform(-1, 1, (3, 3))
+        mu, kappa = rng.uniform(0.5, 2.0, 2)
+        w0 = oracle.neohookean(mu, kappa, F)[0]
+        for _ in range(10):
+            q = rng.normal(size=4)
+            q /= np.linalg.norm(q)
+            a, b, c, d = q
+            R = np.array([[a * a + b * b - c * c - d * d, 2 * (b * c - a * d), 2 * (b * d + a * c)],
+                          [2 * (b * c + a * d), a * a - b * b + c * c - d * d, 2 * (c * d - a * b)],
+                          [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
+            w = oracle.neohookean(mu, kappa, R @ F)[0]
+            assert abs(w - w0) / abs(w + w0 + 1e-4) <= 1e-10
+
+
 def test_major_operator_equals_major_minor_on_minor_symmetric_tensor(oracle):
     """The same (minor-symmetric) tensor in Major storage gives the major-minor
     operator's rows and diagonal."""
