@@ -78,7 +78,7 @@ def test_neohookean_ddw_is_the_gradient_of_dw(oracle):
 
 def test_neohookean_material_frame_indifference(oracle):
     """Model::Solid::Solid::MaterialFrameIndifference (src/Model/Solid/
-    Solid.H:210-262): W(R F) = W(F) for rotations R and det F in [0.5, 2],
+    Solid.H:210-268): W(R F) = W(F) for rotations R and det F in [0.5, 2],
     relative to |W(RF) + W(F)| + 1e-4, tolerance 1e-4 (here far below it)."""
     rng = np.random.default_rng(3)
     for _ in range(10):
