@@ -211,7 +211,7 @@ def cpu_sample(cfg, n_override, C, F0, bc, dx, cycles):
 
 
 def metric_name(n, guess):
-    """The metric string both arms print (the driver pairs them)."""
+    """The metric string both arms print (a comparison pairs them by it)."""
     return ("solve time to 1e-8 rel. residual @%d^3: %smixed FP32/FP64 vs plain FP64; Fapply HBM GB/s"
             % (n, "learned guess + " if guess else ""))
 
