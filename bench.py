@@ -13,8 +13,9 @@ right-hand side and the solve to 1e-8 relative residual (inf-norm of the
 FP64 residual, tol_abs = 0).  Fast path: FGMRES preconditioned by one
 V(1,1)-cycle, both in FP32, inside FP64 iterative refinement, with a direct
 solve on a 5^3-node bottom level.  The plain FP64 comparison is the reference's
-algorithm on the GPU: V(2,2) cycles with damped Jacobi and the BiCGStab
-bottom, everything FP64, from zero.  `value` is seconds per solve (lower is
+algorithm on the GPU: MLMG iterations that are F-cycles (the reference sets
+max_fmg_iter = 100000000) with V(2,2) damped-Jacobi smoothing and the
+BiCGStab bottom, everything FP64, from zero.  `value` is seconds per solve (lower is
 better); `e2e` is the same solve through the C ABI with host buffers
 (stiffness and right-hand side copied in, displacement copied out, inside
 the timed region).
