@@ -9,7 +9,9 @@
   cos(pi x/L) cos(pi y/L) cos(pi z/L) with 32 cells;
 - tests/Eshelby/reference/Eshelby_{displacement,sigma_normal}.csv: the
   analytic Eshelby inclusion solution along x = y = 0.25 to the reference
-  test's tolerance 0.1 (fixture tests/golden/eshelby.json).
+  test's tolerance 0.1 (fixture tests/golden/eshelby.json);
+- tests/TrigTest: the Laplacian model's trigonometric solution along the
+  diagonal to 1e-4, with second-order convergence.
 """
 import json
 import os
@@ -154,3 +156,41 @@ def test_eshelby_known_answer(oracle):
     # the solution is not trivially small: the inclusion's z displacement
     # reaches 0.8 of its analytic peak on the ray
     assert np.abs(u[2]).max() > 0.8 * np.abs(np.array(golden["displacement"]["disp3"])).max() / 1e4
+
+
+def _trig_error(oracle, n):
+    dx = 1.0 / (n - 1)
+    xs = dx * np.arange(n)
+    Z, Y, X = np.meshgrid(xs, xs, xs, indexing="ij")
+    ut = [(P, Q) for P in range(9) for Q in range(P, 9)]
+    C = np.zeros((n, n, n, 45))
+    for q, (P, Q) in enumerate(ut):
+        if P == Q:
+            C[..., q] = 1.0
+    bc = B.Constant()
+    bt, bv = bc.tables()
+    body = np.zeros((3, n, n, n))
+    body[0] = np.sin(np.pi * X) * np.sin(np.pi * Y) * np.sin(np.pi * Z)
+    b = oracle.bc_init(body, bt, bv)
+    rhs = oracle.build_rhs(C, None, bt, np.zeros_like(body), b, dx)
+    u, rep, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_iter=100)
+    assert rep.status == 0
+    d = np.arange(n)
+    exact = -np.sin(np.pi * xs) ** 3 / np.pi ** 2 / 3.0
+    return np.sum((exact - u[0, d, d, d]) ** 2) / np.sum(exact ** 2)
+
+
+def test_trig_known_answer(oracle):
+    """The reference's TrigTest (tests/TrigTest/input, tests/TrigTest/test):
+    the Laplacian model (DDW = alpha, alpha = 1) with the body force
+    b_x = sin(pi x) sin(pi y) sin(pi z) on the unit cube, zero displacement
+    on every face; u_x must match -sin(pi x) sin(pi y) sin(pi z) / (3 pi^2)
+    along the diagonal x = y = z with relative squared error < 1e-4.  The
+    Laplacian's stiffness C_ijkl = delta_ik delta_jl has major but not minor
+    symmetry, so it runs as the 45-value Major tensor with C_PQ = delta_PQ.
+    The reference refines two levels on an explicit mesh; here uniform grids
+    of 33^3 and 65^3 nodes: errors 6.5e-7 and 4.0e-8, the factor 16 of a
+    second-order discretisation in the squared error."""
+    e33, e65 = _trig_error(oracle, 33), _trig_error(oracle, 65)
+    assert e33 < 1e-4 and e65 < 1e-4, (e33, e65)
+    assert 12 < e33 / e65 < 20
