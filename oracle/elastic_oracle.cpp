@@ -47,8 +47,10 @@
 //
 // Pinned against the reference's own known answers (tests/test_oracle_golden.py):
 //   tests/UniaxialTension (linear exactness, 1e-8), tests/Solid/reference/
-//   linear-cubic.dat and affine-cubic.dat (trac_xhi_x(t), 1e-4), and
-//   src/Test/Numeric/Stencil.H:58-106 (derivative accuracy, 1e-2).
+//   linear-cubic.dat and affine-cubic.dat (trac_xhi_x(t), 1e-4),
+//   src/Test/Numeric/Stencil.H:58-106 (derivative accuracy, 1e-2),
+//   tests/Eshelby (analytic inclusion solution, 0.1) and tests/TrigTest
+//   (the Laplacian's trigonometric solution, 1e-4).
 //
 // Layouts: node grid nx*ny*nz, x fastest; vector fields are SoA per component
 // (comp slowest), no ghost nodes.  Stiffness is per node in the reference's
