@@ -98,6 +98,51 @@ def test_neohookean_material_frame_indifference(oracle):
             assert abs(w - w0) / abs(w + w0 + 1e-4) <= 1e-10
 
 
+def test_solid_neo_hookean_series(oracle):
+    """The reference's tests/Solid [neo-hookean] case (tests/Solid/input:69-82,
+    tests/Solid/test): a 4^3-cell unit cube of NeoHookean material mu = 3.0,
+    kappa = 6.5 under the uniaxial_stress tension test with
+    bc.tensiontest.disp = (0,1:0,1), 100 steps of 0.01, solver.nriters = 10;
+    trac_xhi_x(t) -- the first Piola-Kirchhoff P_xx integrated over the x+
+    face -- against tests/Solid/reference/neo-hookean.dat (fixture
+    tests/golden/solid_trac_xhi.json) to the reference test's 1e-4: the
+    oracle's NeoHookean DW/DDW, Major operator, Newton right-hand side and
+    Newton loop reach 9e-7 up to a stretch of 2."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "solid_trac_xhi.json")) as f:
+        ref = json.load(f)["neo-hookean"]
+    rt, rtr = np.array(ref["time"]), np.array(ref["trac_xhi_x"])
+    n, dx = 5, 0.25
+    model = np.empty((n, n, n, 2))
+    model[..., 0], model[..., 1] = 3.0, 6.5
+    bc = B.TensionTest("uniaxial_stress", disp="(0,1:0,1)")
+    u = np.zeros((3, n, n, n))
+    times, trac = [], []
+    for step in range(100):
+        t = 0.01 * step
+        bt, bv = bc.tables(t)
+        b = oracle.bc_init(np.zeros_like(u), bt, bv)
+        du = np.zeros_like(u)
+        for _ in range(10):
+            dw, ddw = oracle.neohookean_field(model, u, dx)
+            rhs = oracle.rhs_dw(dw, bt, u, b, dx)
+            du, rep, _ = oracle.solve(np.ascontiguousarray(ddw), bt, rhs, dx, tol_rel=1e-8, tol_abs=1e-8,
+                                      max_iter=30, x0=du)
+            u = u + du
+        pxx = oracle.neohookean_field(model, u, dx)[0][..., 0]
+        face = pxx[:, :, n - 1]
+        times.append(t)
+        trac.append(0.25 * dx * dx * float((face[:-1, :-1] + face[1:, :-1] + face[:-1, 1:] + face[1:, 1:]).sum()))
+    times, trac = np.array(times), np.array(trac)
+
+    def integrate(x, y):
+        return float(np.sum(0.5 * (y[1:] + y[:-1]) * (x[1:] - x[:-1])))
+    diff = np.interp(times, rt, rtr) - trac
+    err = np.sqrt(integrate(times, diff ** 2)) / np.sqrt(integrate(rt, rtr * rtr))
+    assert err < 1e-4, err
+
+
 def test_major_operator_equals_major_minor_on_minor_symmetric_tensor(oracle):
     """The same (minor-symmetric) tensor in Major storage gives the major-minor
     operator's rows and diagonal."""
