@@ -1,8 +1,9 @@
 """Regenerate the golden fixtures in this folder from the reference checkout.
 
 * solid_trac_xhi.json: the regression data of the 4x4x4-cell tension test
-  (tests/Solid/reference/{linear-cubic,affine-cubic,neo-hookean}.dat of the
-  reference project: columns time, disp_xhi_x, trac_xhi_x).
+  (tests/Solid/reference/{linear-cubic,affine-cubic,affine-hexagonal,
+  neo-hookean}.dat of the reference project: columns time, disp_xhi_x,
+  trac_xhi_x).
 * eshelby.json: the analytic Eshelby curves the reference's Eshelby test
   compares with (tests/Eshelby/reference/Eshelby_displacement.csv, columns
   z, u1..u3 in units of 1e-4; Eshelby_sigma_normal.csv, columns z,
@@ -40,7 +41,7 @@ def write(name, out):
 
 def main(ref_root):
     out = {}
-    for name in ["linear-cubic", "affine-cubic", "neo-hookean"]:
+    for name in ["linear-cubic", "affine-cubic", "affine-hexagonal", "neo-hookean"]:
         d = load(os.path.join(ref_root, "tests", "Solid", "reference", name + ".dat"))
         out[name] = {"time": d["time"], "disp_xhi_x": d["disp_xhi_x"], "trac_xhi_x": d["trac_xhi_x"]}
     out["_source"] = "reference tests/Solid/reference/*.dat (regression data of the 4^3-cell tension test)"

@@ -2,9 +2,10 @@
 
 - tests/UniaxialTension of the reference: linear displacement and constant
   stress to 1e-8 (finite differences are exact on linear fields);
-- tests/Solid/reference/{linear,affine}-cubic.dat: trac_xhi_x(t) of the 4^3
-  cell tension test to the reference test's tolerance 1e-4 (fixture
-  tests/golden/solid_trac_xhi.json, made by tests/golden/make_golden.py);
+- tests/Solid/reference/{linear-cubic,affine-cubic,affine-hexagonal}.dat:
+  trac_xhi_x(t) of the 4^3 cell tension test to the reference test's
+  tolerance 1e-4 (fixture tests/golden/solid_trac_xhi.json, made by
+  tests/golden/make_golden.py);
 - src/Test/Numeric/Stencil.H:58-106: derivative accuracy below 1e-2 on
   cos(pi x/L) cos(pi y/L) cos(pi z/L) with 32 cells;
 - tests/Eshelby/reference/Eshelby_{displacement,sigma_normal}.csv: the
@@ -105,6 +106,50 @@ def test_solid_tension_series(oracle, name, f0):
                                sxx[k + 1, j + 1, n - 1]) * dx * dx
         times.append(t)
         trac.append(tot)
+    times, trac = np.array(times), np.array(trac)
+    diff = np.interp(times, rt, rtr) - trac
+    err = np.sqrt(_integrate(times, diff ** 2)) / np.sqrt(_integrate(rt, rtr * rtr))
+    assert err < 1e-4, err
+
+
+def hexagonal_mm(C11, C12, C13, C33, C44):
+    """The 21 major-minor values of Model::Solid::Linear::Hexagonal at zero
+    Euler angles (src/Model/Solid/Linear/Hexagonal.H:67-111): C1111 = C2222 =
+    C11, C3333 = C33, C1122 = C12, C1133 = C2233 = C13, C2323 = C1313 = C44,
+    and C1212 = (C11 - C12) / 2 (the class's last-written entry, (1,0,1,0))."""
+    pairs = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+    val = {(0, 0, 0, 0): C11, (1, 1, 1, 1): C11, (2, 2, 2, 2): C33, (0, 1, 0, 1): 0.5 * (C11 - C12),
+           (0, 2, 0, 2): C44, (1, 2, 1, 2): C44, (0, 0, 1, 1): C12, (0, 0, 2, 2): C13, (1, 1, 2, 2): C13}
+    return np.array([val.get(pairs[a] + pairs[b], 0.0) for a in range(6) for b in range(a, 6)])
+
+
+def test_solid_affine_hexagonal_series(oracle):
+    """tests/Solid [affine-hexagonal] (tests/Solid/input:31-44): the same
+    tension test with the hexagonal model C11 = 0.597, C12 = 0.262, C13 =
+    0.217, C33 = 0.617, C44 = 0.164 and eigenstrain 0.001 I -- a major-minor
+    tensor with five distinct constants, and a nonzero traction at t = 0 from
+    the eigenstrain alone -- against affine-hexagonal.dat to 1e-4 (1.1e-6)."""
+    with open(os.path.join(GOLDEN, "solid_trac_xhi.json")) as f:
+        ref = json.load(f)["affine-hexagonal"]
+    rt, rtr = np.array(ref["time"]), np.array(ref["trac_xhi_x"])
+    n, dx = 5, 0.25
+    C = np.empty((n, n, n, 21))
+    C[...] = hexagonal_mm(0.597, 0.262, 0.217, 0.617, 0.164)
+    F0 = np.full((n, n, n), 0.001)
+    bc = B.TensionTest("uniaxial_stress", disp="(0,1:0,0.01)")
+    u = np.zeros((3, n, n, n))
+    times, trac = [], []
+    for step in range(100):
+        t = 0.01 * step
+        bt, bv = bc.tables(t)
+        b = oracle.bc_init(np.zeros_like(u), bt, bv)
+        rhs = oracle.build_rhs(C, F0, bt, u, b, dx)
+        du, rep, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-8, tol_abs=1e-8, max_iter=30)
+        u = u + du
+        s, _, _ = oracle.stress_strain(C, F0, u, dx)
+        face = s[..., 0][:, :, n - 1]
+        times.append(t)
+        trac.append(0.25 * dx * dx * float((face[:-1, :-1] + face[1:, :-1] + face[:-1, 1:] + face[1:, 1:]).sum()))
     times, trac = np.array(times), np.array(trac)
     diff = np.interp(times, rt, rtr) - trac
     err = np.sqrt(_integrate(times, diff ** 2)) / np.sqrt(_integrate(rt, rtr * rtr))
