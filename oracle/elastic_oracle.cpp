@@ -47,9 +47,9 @@
 //
 // Pinned against the reference's own known answers (tests/test_oracle_golden.py):
 //   tests/UniaxialTension (linear exactness, 1e-8), tests/Solid/reference/
-//   linear-cubic.dat, affine-cubic.dat, affine-hexagonal.dat and
-//   neo-hookean.dat (trac_xhi_x(t), 1e-4; tests/test_neohookean.py for the
-//   last),
+//   linear-cubic.dat, affine-cubic.dat, affine-hexagonal.dat,
+//   transverselyisotropic.dat and neo-hookean.dat (trac_xhi_x(t), 1e-4;
+//   tests/test_neohookean.py for the last),
 //   src/Test/Numeric/Stencil.H:58-106 (derivative accuracy, 1e-2),
 //   tests/Eshelby (analytic inclusion solution, 0.1) and tests/TrigTest
 //   (the Laplacian's trigonometric solution, 1e-4).

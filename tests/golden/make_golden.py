@@ -2,8 +2,8 @@
 
 * solid_trac_xhi.json: the regression data of the 4x4x4-cell tension test
   (tests/Solid/reference/{linear-cubic,affine-cubic,affine-hexagonal,
-  neo-hookean}.dat of the reference project: columns time, disp_xhi_x,
-  trac_xhi_x).
+  transverselyisotropic,neo-hookean}.dat of the reference project: columns
+  time, disp_xhi_x, trac_xhi_x).
 * eshelby.json: the analytic Eshelby curves the reference's Eshelby test
   compares with (tests/Eshelby/reference/Eshelby_displacement.csv, columns
   z, u1..u3 in units of 1e-4; Eshelby_sigma_normal.csv, columns z,
@@ -41,7 +41,7 @@ def write(name, out):
 
 def main(ref_root):
     out = {}
-    for name in ["linear-cubic", "affine-cubic", "affine-hexagonal", "neo-hookean"]:
+    for name in ["linear-cubic", "affine-cubic", "affine-hexagonal", "transverselyisotropic", "neo-hookean"]:
         d = load(os.path.join(ref_root, "tests", "Solid", "reference", name + ".dat"))
         out[name] = {"time": d["time"], "disp_xhi_x": d["disp_xhi_x"], "trac_xhi_x": d["trac_xhi_x"]}
     out["_source"] = "reference tests/Solid/reference/*.dat (regression data of the 4^3-cell tension test)"

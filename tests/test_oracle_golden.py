@@ -2,7 +2,8 @@
 
 - tests/UniaxialTension of the reference: linear displacement and constant
   stress to 1e-8 (finite differences are exact on linear fields);
-- tests/Solid/reference/{linear-cubic,affine-cubic,affine-hexagonal}.dat:
+- tests/Solid/reference/{linear-cubic,affine-cubic,affine-hexagonal,
+  transverselyisotropic}.dat:
   trac_xhi_x(t) of the 4^3 cell tension test to the reference test's
   tolerance 1e-4 (fixture tests/golden/solid_trac_xhi.json, made by
   tests/golden/make_golden.py);
@@ -123,19 +124,24 @@ def hexagonal_mm(C11, C12, C13, C33, C44):
     return np.array([val.get(pairs[a] + pairs[b], 0.0) for a in range(6) for b in range(a, 6)])
 
 
-def test_solid_affine_hexagonal_series(oracle):
-    """tests/Solid [affine-hexagonal] (tests/Solid/input:31-44): the same
-    tension test with the hexagonal model C11 = 0.597, C12 = 0.262, C13 =
-    0.217, C33 = 0.617, C44 = 0.164 and eigenstrain 0.001 I -- a major-minor
-    tensor with five distinct constants, and a nonzero traction at t = 0 from
-    the eigenstrain alone -- against affine-hexagonal.dat to 1e-4 (1.1e-6)."""
+@pytest.mark.parametrize("name,consts,f0", [
+    ("affine-hexagonal", (0.597, 0.262, 0.217, 0.617, 0.164), 0.001),
+    ("transverselyisotropic", (168.3, 1.221, 1.0, 160.0, 0.757), None)])
+def test_solid_hexagonal_series(oracle, name, consts, f0):
+    """tests/Solid [affine-hexagonal] (tests/Solid/input:31-44) and
+    [linear-transverse] (:108-120): the same tension test with the hexagonal
+    model (eigenstrain 0.001 I: a nonzero traction already at t = 0) and the
+    transversely isotropic one (Set::Matrix4<3,MajorMinor>::Transverse,
+    src/Set/Matrix4_MajorMinor.H:564-611, the same table) -- major-minor
+    tensors with five distinct constants -- against their .dat series to
+    1e-4 (1.1e-6 and 1.9e-6)."""
     with open(os.path.join(GOLDEN, "solid_trac_xhi.json")) as f:
-        ref = json.load(f)["affine-hexagonal"]
+        ref = json.load(f)[name]
     rt, rtr = np.array(ref["time"]), np.array(ref["trac_xhi_x"])
     n, dx = 5, 0.25
     C = np.empty((n, n, n, 21))
-    C[...] = hexagonal_mm(0.597, 0.262, 0.217, 0.617, 0.164)
-    F0 = np.full((n, n, n), 0.001)
+    C[...] = hexagonal_mm(*consts)
+    F0 = None if f0 is None else np.full((n, n, n), f0)
     bc = B.TensionTest("uniaxial_stress", disp="(0,1:0,0.01)")
     u = np.zeros((3, n, n, n))
     times, trac = [], []
