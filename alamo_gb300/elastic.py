@@ -325,7 +325,7 @@ def _flag(v):
     return bool(v)
 
 
-def parse_solver_opts(kv, opts=None):
+def parse_solver_opts(kv, opts=None, newton=False):
     """``Linear::Parse`` (src/Solver/Nonlocal/Linear.H:296-382) and
     ``PrepareMLMG`` (:255-290): the reference's ``solver.*`` keys (given
     without the prefix) onto an agb_solver_opts, starting from ``opts`` or
@@ -333,9 +333,13 @@ def parse_solver_opts(kv, opts=None):
     "abort_on_fail"} for the keys that are arguments of the solve.  The
     deprecated keys abort in the reference and raise ValueError here, as do
     unknown keys and the CG bottom solver (not provided: BiCGStab, the direct
-    bottom and the smoother are)."""
+    bottom and the smoother are).  newton=True also takes Newton::Parse's
+    nriters and nrtolerance (src/Solver/Nonlocal/Newton.H:643-652) into
+    extra."""
     o = default_opts() if opts is None else opts
     extra = {"tol_rel": None, "tol_abs": None, "abort_on_fail": True}
+    if newton:
+        extra.update(nriters=None, nrtolerance=None)
     for k, v in kv.items():
         if k in ("max_fixed_iter", "cg_tol_rel", "cg_tol_abs"):
             raise ValueError(k + " is deprecated in the reference (Linear.H:308-335)")
@@ -355,6 +359,10 @@ def parse_solver_opts(kv, opts=None):
             extra["abort_on_fail"] = _flag(v)
         elif k in _NO_EFFECT_KEYS:
             pass
+        elif newton and k == "nriters":
+            extra["nriters"] = int(v)
+        elif newton and k == "nrtolerance":
+            extra["nrtolerance"] = float(v)
         else:
             raise KeyError("unknown solver key " + k)
     return o, extra
@@ -424,6 +432,22 @@ class Newton(Linear):
         super().__init__(op)
         self.nriters = int(nriters)
         self.nrtolerance = float(nrtolerance)
+
+    def setNRIters(self, n):
+        """Newton::setNRIters (src/Solver/Nonlocal/Newton.H:44)."""
+        self.nriters = int(n)
+
+    def Parse(self, kv):
+        """Newton::Parse (src/Solver/Nonlocal/Newton.H:643-652): the linear
+        solver keys plus nriters and nrtolerance."""
+        o, extra = parse_solver_opts(kv, self.op.opts, newton=True)
+        self.op.SetOpts(o)
+        if extra["nriters"] is not None:
+            self.nriters = extra["nriters"]
+        if extra["nrtolerance"] is not None:
+            self.nrtolerance = extra["nrtolerance"]
+        self.parsed = extra
+        return extra
 
     def setPsi(self, psi, small=1e-8):
         """Newton::setPsi (src/Solver/Nonlocal/Newton.H:46-49): the operator's

@@ -64,3 +64,14 @@ def test_create_rejects_bad_fgmres_options(agb, field, value):
     h = ctypes.c_void_p()
     dx = (ctypes.c_double * 3)(1, 1, 1)
     assert agb.lib().agb_elastic_create(ctypes.byref(h), 5, 5, 5, dx, 0, ctypes.byref(o)) == _lib.AGB_BAD_ARG
+
+
+def test_parse_newton_keys(agb):
+    """Newton::Parse adds nriters and nrtolerance to the linear keys
+    (src/Solver/Nonlocal/Newton.H:643-652; defaults 1 and 0, :630-631); the
+    linear solver refuses them."""
+    from alamo_gb300.elastic import parse_solver_opts
+    o, extra = parse_solver_opts({"nriters": "10", "nrtolerance": "1e-6", "max_iter": 30}, newton=True)
+    assert (extra["nriters"], extra["nrtolerance"], o.max_iter) == (10, 1e-6, 30)
+    with pytest.raises(KeyError):
+        parse_solver_opts({"nriters": 10})
