@@ -15,6 +15,7 @@ EXPORTS = [
     "agb_elastic_set_stream", "agb_elastic_set_model", "agb_elastic_get_model", "agb_elastic_set_bc",
     "agb_elastic_prepare", "agb_elastic_num_levels", "agb_elastic_level_dims", "agb_elastic_fapply",
     "agb_elastic_fapply_f32", "agb_elastic_diagonal", "agb_elastic_fsmooth", "agb_elastic_residual",
+    "agb_elastic_fsmooth_f32", "agb_elastic_residual_f32",
     "agb_elastic_restrict", "agb_elastic_prolong_add", "agb_elastic_vcycle", "agb_elastic_bc_init", "agb_elastic_build_rhs",
     "agb_linear_solve", "agb_newton_solve", "agb_elastic_stress_strain", "agb_profile_enable",
     "agb_profile_reset", "agb_profile_get", "agb_launch_count", "agb_cubic_stiffness", "agb_synth_uniform",

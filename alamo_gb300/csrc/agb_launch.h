@@ -160,14 +160,6 @@ cudaError_t launch_dense_bottom(const double* Ainv, const double* rhs, double* s
 }  // namespace agb
 
 namespace agb {
-// z-marching fine-level stencil kernel: mode 0 = Fapply (out = A x),
-// 1 = damped-Jacobi sweep (needs b, dg, omega), 2 = residual (out = b - A x)
-template <typename T>
-cudaError_t launch_zmarch(int mode, int sym, const T* x, const T* C, const LevelGeom<T>& G, const BcTable& bc,
-                          const T* b, const T* dg, T omega, T* out, cudaStream_t s);
-}  // namespace agb
-
-namespace agb {
 // message returned by agb_last_error() for the calling thread
 void set_last_error(const char* msg);
 }  // namespace agb

@@ -492,15 +492,14 @@ template <>
 struct Fam<float> { enum { J = AGB_K_JACOBI_F32, R = AGB_K_RESIDUAL_F32 }; };
 
 // the z-marching kernels serve FP32 levels (FP64 stays on the per-node
-// kernels: it is FP64-pipe bound and the z-march form spills):
-// fine_kernel 0: the TMA-staged kernels on every level large enough (see
-// build_f32); 2: the register-staged ones on the fine level; 1: none
+// kernels: it is FP64-pipe bound): fine_kernel 0: the TMA-staged kernels on
+// every level large enough (see build_f32); 1: none
 template <typename T>
 bool use_zm(const agb_elastic*, const Lev<T>&, int) { return false; }
 template <>
-bool use_zm<float>(const agb_elastic* h, const Lev<float>& v, int l) {
+bool use_zm<float>(const agb_elastic* h, const Lev<float>& v, int) {
     if (h->psi_set || h->sym == SYM_MAJ) return false;
-    return h->opts.fine_kernel == 0 ? v.tma : (h->opts.fine_kernel == 2 && l == 0);
+    return h->opts.fine_kernel == 0 && v.tma;
 }
 
 // FP32 z-marching stencil on a level: mode 0 out = A x, 1 one Jacobi sweep,
@@ -510,21 +509,18 @@ cudaError_t level_zm(agb_elastic* h, const Lev<T>& v, int mode, const T* x, cons
 template <>
 cudaError_t level_zm<float>(agb_elastic* h, const Lev<float>& v, int mode, const float* x, const float* b,
                             const float* dg, float omega, float* out) {
-    if (v.tma && h->opts.fine_kernel == 0) {
-        // faces and interior on the library's stream: running the faces on a
-        // second stream beside the interior sweep measured slower (the face
-        // blocks take SM slots the marching blocks need)
-        h->launches++;  // interior + faces
-        // the TMA kernels' Jacobi form takes the inverse diagonal
-        return launch_zmarch_tma(mode, h->sym, v.map, x, v.C, v.G, h->bc, b, mode == 1 ? v.dinv : dg, omega, out,
-                                 h->bottom_info + 3, h->stream, nullptr);
-    }
-    return launch_zmarch<float>(mode, h->sym, x, v.C, v.G, h->bc, b, dg, omega, out, h->stream);
+    // faces and interior on the library's stream: running the faces on a
+    // second stream beside the interior sweep measured slower (the face
+    // blocks take SM slots the marching blocks need)
+    h->launches++;  // interior + faces
+    // the TMA kernels' Jacobi form takes the inverse diagonal
+    return launch_zmarch_tma(mode, h->sym, v.map, x, v.C, v.G, h->bc, b, mode == 1 ? v.dinv : dg, omega, out,
+                             h->bottom_info + 3, h->stream, nullptr);
 }
 template <>
-cudaError_t level_zm<double>(agb_elastic* h, const Lev<double>& v, int mode, const double* x, const double* b,
-                             const double* dg, double omega, double* out) {
-    return launch_zmarch<double>(mode, h->sym, x, v.C, v.G, h->bc, b, dg, omega, out, h->stream);
+cudaError_t level_zm<double>(agb_elastic*, const Lev<double>&, int, const double*, const double*, const double*,
+                             double, double*) {
+    return cudaErrorNotSupported;  // never selected: use_zm<double> is false
 }
 
 // ncalls Fsmooth calls (2 sweeps each) on level l; cor_zero: cor is known 0
@@ -1068,7 +1064,7 @@ static agb_status check_opts(const agb_solver_opts* o) {
     if (o->solver != AGB_SOLVER_VCYCLE && o->solver != AGB_SOLVER_FGMRES) return fail(AGB_BAD_ARG, "unknown solver");
     if (o->bottom_solver < AGB_BOTTOM_BICGSTAB || o->bottom_solver > AGB_BOTTOM_SMOOTHER)
         return fail(AGB_BAD_ARG, "unknown bottom solver");
-    if (o->fine_kernel < 0 || o->fine_kernel > 2) return fail(AGB_BAD_ARG, "fine_kernel must be 0, 1 or 2");
+    if (o->fine_kernel < 0 || o->fine_kernel > 1) return fail(AGB_BAD_ARG, "fine_kernel must be 0 or 1");
     if (o->tma_min_nodes < 0) return fail(AGB_BAD_ARG, "tma_min_nodes must be >= 0");
     if (o->solver == AGB_SOLVER_FGMRES && (o->krylov_dim < 1 || o->krylov_dim > 39))
         return fail(AGB_BAD_ARG, "krylov_dim must lie in [1, 39]");
@@ -1382,6 +1378,52 @@ agb_status agb_elastic_residual(agb_elastic* h, int level, const double* x, cons
     CK(cudaMemcpyAsync(h->norms_host, h->norms_dev, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     TRY(finish_out(h, r, dr, bytes, where));
     if (norms) { norms[0] = h->norms_host[0]; norms[1] = h->norms_host[1]; }
+    prof_collect(h);
+    return AGB_OK;
+}
+
+agb_status agb_elastic_fsmooth_f32(agb_elastic* h, int level, float* x, const float* b, int ncalls, int where) {
+    TRY(check_level(h, level));
+    if (!x || !b || ncalls < 0) return fail(AGB_BAD_ARG, "bad argument");
+    TRY(ensure_f32(h));
+    Lev<float>& v = h->L32[level];
+    const size_t bytes = sizeof(float) * 3 * v.G.N;
+    const void* dx0 = nullptr;
+    const void* db = nullptr;
+    TRY(dev_in(h, 0, x, bytes, where, &dx0));
+    TRY(dev_in(h, 1, b, bytes, where, &db));
+    CK(cudaMemcpyAsync(v.cor, dx0, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(v.res, db, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    TRY(smooth<float>(h, h->L32, level, ncalls, false));
+    if (where == AGB_MEM_HOST) CK(cudaMemcpyAsync(x, v.cor, bytes, cudaMemcpyDeviceToHost, h->stream));
+    else CK(cudaMemcpyAsync(x, v.cor, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    prof_collect(h);
+    return AGB_OK;
+}
+
+agb_status agb_elastic_residual_f32(agb_elastic* h, int level, const float* x, const float* b, float* r, int where) {
+    TRY(check_level(h, level));
+    if (!x || !b || !r) return fail(AGB_BAD_ARG, "null argument");
+    TRY(ensure_f32(h));
+    Lev<float>& v = h->L32[level];
+    const size_t bytes = sizeof(float) * 3 * v.G.N;
+    const void* dx0 = nullptr;
+    const void* db = nullptr;
+    void* dr = nullptr;
+    TRY(dev_in(h, 0, x, bytes, where, &dx0));
+    TRY(dev_in(h, 1, b, bytes, where, &db));
+    TRY(dev_out(h, 2, r, bytes, where, &dr));
+    {
+        ProfScope ps(h, AGB_K_RESIDUAL_F32, level == 0);
+        if (use_zm<float>(h, v, level))
+            CK(level_zm<float>(h, v, 2, (const float*)dx0, (const float*)db, nullptr, 0.f, (float*)dr));
+        else
+            CK(launch_residual<float>(h->sym, (const float*)dx0, (const float*)db, v.C, v.G, h->bc, (float*)dr,
+                                      nullptr, nullptr, h->stream));
+    }
+    h->launches++;
+    TRY(finish_out(h, r, dr, bytes, where));
     prof_collect(h);
     return AGB_OK;
 }

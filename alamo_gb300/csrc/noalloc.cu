@@ -1,21 +1,25 @@
 // Allocation-free residual with norms.
 //
-// For callers that cannot call cudaMalloc: code running inside a CUDA graph
-// capture or another library's stream callback, code whose memory is owned
-// by a pool they must not grow, or an embedding (a plugin inside a host code
-// that reserves the whole device up front).  They pass their own inputs and
-// outputs; the per-block partial norms this kernel needs live in a fixed
-// array in the library's device image instead of in allocated memory.
+// For callers that cannot call cudaMalloc.  Examples: a host code whose
+// memory arena reserved the whole device at start-up (nothing is left to
+// allocate), a plugin that lives inside such a code, and a time-stepping
+// loop that must not call cudaMalloc/cudaFree between steps because those
+// calls can synchronise the whole device and stall its other streams.  They
+// pass their own inputs and outputs; the per-block partial norms this kernel
+// needs live in a fixed array in the library's device image instead of in
+// allocated memory.
 //
 // The scratch array is file-scope device memory of AGB_NOALLOC_MAX_BLOCKS
-// pairs of doubles (2 MiB); every GPU that loads the library holds it until
-// the process exits.  In host code the array's name is only a host-side
-// handle, so the device address is looked up with cudaGetSymbolAddress, once
-// per device, by the first call made with that device current (do that first
-// call before any stream capture).  Every call uses the same array and leaves
-// its contents behind: the kernels overwrite every entry they later read, and
-// two calls that overlap on the GPU (different streams, no ordering) race on
-// it and produce wrong norms.
+// pairs of doubles plus the two final norms (2 MiB); every GPU that loads
+// the library holds it until the process exits.  In host code the array's
+// name is only a host-side stand-in, so its device address is looked up
+// with cudaGetSymbolAddress, once per device, by the first call made with
+// that device current, and cached.  A device reset (cudaDeviceReset) after
+// that first call is not supported: the cached address would be stale.
+// Every call uses the same array and leaves its contents behind: the
+// kernels overwrite every entry they later read, and two calls that overlap
+// on the GPU (different streams, no ordering) race on it and produce wrong
+// norms.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -27,7 +31,6 @@
 
 namespace agb {
 
-static constexpr int NA_BX = 32, NA_BY = 4, NA_BZ = 2;  // the residual kernel's block shape
 static constexpr int NA_MAX_DEVICES = 64;
 
 // partial (max, sum of squares) per block, then the two final norms
@@ -57,11 +60,12 @@ extern "C" agb_status agb_residual_norms_noalloc(int nx, int ny, int nz, const d
     if (nx < 3 || ny < 3 || nz < 3 || !dx || !(dx[0] > 0) || !(dx[1] > 0) || !(dx[2] > 0)) return AGB_BAD_ARG;
     if (sym != AGB_SYM_ISOTROPIC && sym != AGB_SYM_MAJORMINOR) return AGB_BAD_ARG;
     if (!C_soa || !bc_type || !x || !b || !r || !norms) return AGB_BAD_ARG;
-    const int64_t nblocks = (int64_t)((nx + NA_BX - 1) / NA_BX) * ((ny + NA_BY - 1) / NA_BY) * ((nz + NA_BZ - 1) / NA_BZ);
+    // the residual kernel's own block count (one partial pair per block)
+    const int64_t nblocks = residual_blocks(nx, ny, nz);
     if (nblocks > AGB_NOALLOC_MAX_BLOCKS) {
         char msg[160];
         std::snprintf(msg, sizeof msg,
-                      "agb_residual_norms_noalloc: the grid needs %lld blocks of 32x4x2 nodes; the fixed scratch "
+                      "agb_residual_norms_noalloc: the grid needs %lld residual blocks; the fixed scratch "
                       "holds %d (AGB_NOALLOC_MAX_BLOCKS)",
                       (long long)nblocks, AGB_NOALLOC_MAX_BLOCKS);
         set_last_error(msg);
@@ -80,6 +84,12 @@ extern "C" agb_status agb_residual_norms_noalloc(int nx, int ny, int nz, const d
     const LevelGeom<double> G = make_geom<double>(nx, ny, nz, dx);
     int nb = 0;
     if (launch_residual<double>(sym, x, b, C_soa, G, bc, r, scratch, &nb, s) != cudaSuccess) return AGB_CUDA_ERROR;
+    if (nb < 1 || nb > AGB_NOALLOC_MAX_BLOCKS) {
+        // unreachable while residual_blocks() describes the launch; the
+        // partials would have run past the fixed array
+        set_last_error("agb_residual_norms_noalloc: residual launch used more blocks than the fixed scratch holds");
+        return AGB_LIMIT;
+    }
     double* fin = scratch + 2 * AGB_NOALLOC_MAX_BLOCKS;
     if (launch_reduce_norms(scratch, nb, fin, s) != cudaSuccess) return AGB_CUDA_ERROR;
     if (cudaMemcpyAsync(norms, fin, 2 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess)

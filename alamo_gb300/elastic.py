@@ -187,6 +187,23 @@ class Elastic:
         L.check(L.lib().agb_elastic_fsmooth(self.h, int(level), px, pb, int(ncalls), _same_where(wx, wb)))
         return x
 
+    def Fsmooth_f32(self, x, b, ncalls=1, level=0):
+        """The mixed-precision cycle's FP32 Fsmooth, in place on x (float32)."""
+        px, wx = _arg(x, np.float32)
+        pb, wb = _arg(b, np.float32)
+        L.check(L.lib().agb_elastic_fsmooth_f32(self.h, int(level), px, pb, int(ncalls), _same_where(wx, wb)))
+        return x
+
+    def residual_f32(self, x, b, r=None, level=0):
+        """The mixed-precision cycle's FP32 residual r = b - A x (float32)."""
+        if r is None:
+            r = np.empty(self._vec_shape(level), dtype=np.float32)
+        px, wx = _arg(x, np.float32)
+        pb, wb = _arg(b, np.float32)
+        pr, wr = _arg(r, np.float32)
+        L.check(L.lib().agb_elastic_residual_f32(self.h, int(level), px, pb, pr, _same_where(wx, wb, wr)))
+        return r
+
     def residual(self, x, b, r=None, level=0):
         """r = b - A x; returns (r, (inf-norm, 2-norm))."""
         if r is None:

@@ -3,7 +3,8 @@
 Workload (default, --config c2): 257^3 nodes on the unit cube, a cubic
 Voronoi polycrystal of 64 grains (C11=1.68, C12=1.21, C44=0.75, Haar-random
 rotations), uniaxial_stress_clamp loading u_x = 0.01 on the x+ face; stiffness
-is major-minor (21 values per node).  Synthetic inputs, seeded.
+is major-minor (21 values per node).  Synthetic inputs, seeded, generated in
+numpy (alamo_gb300/workloads.py) so both arms see the same bytes.
 
 One step = one complete solve from the inputs resident in HBM: SetModel
 (stiffness layout change), prepareForSolve (stiffness coarsening, diagonals,
@@ -12,16 +13,25 @@ with its residual-based fallback to zero; --guess '' skips it), the Newton
 right-hand side and the solve to 1e-8 relative residual (inf-norm of the
 FP64 residual, tol_abs = 0).  Fast path: FGMRES preconditioned by one
 V(1,1)-cycle, both in FP32, inside FP64 iterative refinement, with a direct
-solve on a 5^3-node bottom level.  The plain FP64 comparison is the reference's
-algorithm on the GPU: MLMG iterations that are F-cycles (the reference sets
-max_fmg_iter = 100000000) with V(2,2) damped-Jacobi smoothing and the
-BiCGStab bottom, everything FP64, from zero.  `value` is seconds per solve (lower is
-better); `e2e` is the same solve through the C ABI with host buffers
-(stiffness and right-hand side copied in, displacement copied out, inside
-the timed region).
+solve on a 5^3-node bottom level.  Two FP64 GPU comparisons: the reference's
+algorithm (MLMG iterations that are F-cycles -- the reference sets
+max_fmg_iter = 100000000 -- with V(2,2) damped-Jacobi smoothing and the
+BiCGStab bottom, from zero), and FP64 FGMRES(V(1,1)) with the same direct
+5^3 bottom as the fast path (what the solver choice buys without FP32).
+`value` is seconds per solve (lower is better); `e2e` is the same solve
+through the C ABI with host buffers (stiffness and right-hand side copied
+in, displacement copied out, inside the timed region).
 
---impl reference times the reference's CPU path restated in oracle/ (the
-reference itself needs AMReX and cannot be built) on all host cores.
+The CPU leg runs the reference's CPU path, restated in oracle/ (the
+reference itself needs AMReX and cannot be built), on all host cores: one
+whole FP64 solve to 1e-8 with the reference's solver settings, timed, then
+continued to 1e-12 (untimed) as the FP64 oracle solution every GPU result's
+error is stated against.  --impl reference times that same whole solve.
+
+Other workloads (--extra, on by default): config 1 (33^3 inclusion: Fapply
+and solve against the oracle), config 3 (513^3 spheres, mixed against FP64),
+config 4 (held-out learned-guess evaluation at 129^3 and 257^3) and config 5
+(256-grain polycrystal, learned guess + mixed against FP64).
 """
 import argparse
 import json
@@ -36,13 +46,6 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# FP64 multigrid iterations the reference algorithm needs to reach 1e-8 on
-# each workload: F-cycles, since Linear::PrepareMLMG sets max_fmg_iter to
-# 100000000 (the oracle and the GPU FP64 path iterate identically); used to
-# scale the CPU sample to a whole solve when the run has no plain FP64 solve
-# of its own to count them.
-FP64_CYCLES = {"c1": 18, "c2": 50, "c3": 16}
-
 # bytes each kernel family must move per fine-level node (each array once)
 BYTES_PER_NODE = {
     "jacobi_f32": {2: 56, 21: 132},
@@ -55,16 +58,18 @@ BYTES_PER_NODE = {
 FAMILY = {"fapply_f64": 0, "jacobi_f64": 1, "residual_f64": 2, "fapply_f32": 3, "jacobi_f32": 4, "residual_f32": 5,
           "restrict": 6, "prolong": 7, "bottom": 8}
 # dram__bytes_read.sum + dram__bytes_write.sum of one fine-level Jacobi
-# sweep from 129^3 captures: the interior sweep per node (284.7 MB + 20.3 MB
-# over 2,146,689 nodes, profiles/k_zmarch_tma_jacobi_mm_129.md; it streams
-# every array once, so it scales with the nodes) and the boundary-face
-# kernel per boundary node (28.1 MB + 0.1 MB over 98,306 boundary nodes,
-# profiles/k_zt_faces_mm_129.md); (per node, per boundary node).  The
+# sweep, from ncu captures at 129^3: the interior sweep per node (284.7 MB +
+# 20.3 MB over 2,146,689 nodes; it streams every array once, so it scales
+# with the nodes) and the boundary-face kernel per boundary node (28.1 MB +
+# 0.1 MB over 98,306 boundary nodes); (per node, per boundary node).  The
 # isotropic sweep's interior from a 257^3 capture (757.9 MB + 183.8 MB over
-# 16,974,593 nodes, profiles/k_zmarch_tma_jacobi_iso_257.md); its faces were
-# not captured (None: the figure is the interior sweep's alone)
+# 16,974,593 nodes); its faces were not captured (None: the figure is the
+# interior sweep's alone)
 TRAFFIC_PER_NODE = {("jacobi_f32", 21): ((284.697344e6 + 20.251904e6) / 2146689, (28.08704e6 + 0.097536e6) / 98306),
                     ("jacobi_f32", 2): ((757.910784e6 + 183.846656e6) / 16974593, None)}
+TOL = 1e-8          # the metric's relative residual
+ORACLE_TOL = 1e-12  # the FP64 oracle solution errors are stated against
+REF_BUDGET_S = 150.0  # --impl reference: start another whole solve only within this
 
 
 def parse():
@@ -81,9 +86,12 @@ def parse():
     p.add_argument("--krylov", type=int, default=20)
     p.add_argument("--pre", type=int, default=1, help="Fsmooth calls before restriction in the FP32 V-cycle")
     p.add_argument("--post", type=int, default=1, help="Fsmooth calls after prolongation in the FP32 V-cycle")
-    p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison solve")
-    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    p.add_argument("--smoother", default="jacobi", choices=["jacobi", "gs"],
+                   help="FP32 smoother: damped Jacobi (the reference's) or multicolour Gauss-Seidel")
+    p.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison solves")
+    p.add_argument("--no-cpu", action="store_true", help="skip the oracle (CPU baseline and error reference)")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-extra", action="store_true", help="skip configs 1, 3, 4 and 5")
     p.add_argument("--n", type=int, default=0, help="override the grid size (nodes per axis)")
     p.add_argument("--guess", default=os.path.join(ROOT, "alamo_gb300", "weights", "unet65.npy"),
                    help="U-Net weights of the learned initial guess ('' = solve from zero)")
@@ -91,24 +99,30 @@ def parse():
 
 
 def workload(cfg, n_override=0):
-    """(name, n, C, F0, bc, dx, sym)"""
+    """(name, n, C, F0, bc, dx) from the numpy generators (no CUDA library)."""
     from alamo_gb300 import bc as B
-    from alamo_gb300 import synth
+    from alamo_gb300 import workloads as W
     if cfg == "c1":
         n = n_override or 33
-        C, F0, dx = synth.inclusion_iso(n)
-        return ("c1: 33^3 isotropic inclusion r=0.25 contrast 10, eigenstrain 0.01 I, zero-displacement faces",
+        C, F0, dx = W.inclusion_iso(n)
+        return ("c1: %d^3 isotropic inclusion r=0.25 contrast 10, eigenstrain 0.01 I, zero-displacement faces" % n,
                 n, C, F0, B.Constant(), dx)
     if cfg == "c2":
         n = n_override or 257
-        C, dx = synth.voronoi_cubic(n, 64, seed=1)
+        C, dx = W.voronoi_cubic(n, 64, seed=1)
         return ("c2: %d^3 cubic Voronoi polycrystal, 64 grains, C11/C12/C44=1.68/1.21/0.75, "
                 "uniaxial_stress_clamp u_x=0.01" % n, n, C, None, B.TensionTest("uniaxial_stress_clamp", disp=0.01),
                 dx)
     n = n_override or 513
-    C, F0, dx, placed = synth.spheres_diffuse(n, 200, seed=3)
+    C, F0, dx, placed = W.spheres_diffuse(n, 200, seed=3)
     return ("c3: %d^3 isotropic two-phase, %d spheres r in [0.02,0.06] with a diffuse interface of 4 node spacings, "
             "contrast 10, eigenstrain U[0,0.02]" % (n, placed), n, C, F0, B.Constant(), dx)
+
+
+def config_dict(name, n, C):
+    """The workload description both arms print (identical on both)."""
+    return {"workload": name, "nodes": n ** 3, "tolerance": "%g relative inf-norm residual, tol_abs 0" % TOL,
+            "l2": "inputs larger than L2 (%.1f GB of stiffness), no flush needed" % (C.nbytes / 1e9)}
 
 
 class Clocks:
@@ -170,17 +184,37 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-# --------------------------------------------------------------- CPU sample
-def cpu_sample(cfg, n_override, C, F0, bc, dx, cycles):
-    """Oracle (the reference's CPU path restated) on all host threads: time
-    the right-hand side, the hierarchy set-up and six fixed F-cycles (the
-    reference's MLMG iteration), and scale the per-cycle time to the FP64
-    cycle count of the whole solve."""
+def nlevels(n):
+    lev, m = 1, n
+    while (m - 1) % 2 == 0 and (m - 1) // 2 >= 2:
+        m = (m - 1) // 2 + 1
+        lev += 1
+    return lev
+
+
+def rel_err(u, ref):
+    """{rel_inf, rel_l2} of u against ref."""
+    d = np.asarray(u) - np.asarray(ref)
+    return {"rel_inf": float(np.abs(d).max() / max(np.abs(ref).max(), 1e-300)),
+            "rel_l2": float(np.sqrt((d * d).sum()) / max(np.sqrt((np.asarray(ref) ** 2).sum()), 1e-300))}
+
+
+# --------------------------------------------------------------- the oracle
+def load_oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
     threads = os.cpu_count() or 1
     O.set_threads(threads)
+    return O, threads
+
+
+def oracle_solve(O, C, F0, bc, dx, refine=True):
+    """The reference's CPU path (oracle restatement) on all host threads:
+    Newton right-hand side at u = 0, then the FP64 MLMG solve with the
+    reference's settings (F-cycles, V(2,2), BiCGStab bottom, full
+    coarsening) to 1e-8, timed; with refine, continued to 1e-12 (untimed)
+    for the error reference.  Returns (x_1e-8, x_1e-12 or None, info)."""
     n = C.shape[0]
     bt, bv = bc.tables()
     u = np.zeros((3, n, n, n))
@@ -188,27 +222,54 @@ def cpu_sample(cfg, n_override, C, F0, bc, dx, cycles):
     b = O.bc_init(u, bt, bv)
     rhs = O.build_rhs(C, F0, bt, u, b, dx)
     t_rhs = time.perf_counter() - t0
-    sample_cycles = 6
-    x, rep, _ = O.solve(C, bt, rhs, dx, fixed_iter=sample_cycles)
-    per_cycle = (rep.seconds - rep.setup_seconds) / sample_cycles
-    setup = rep.setup_seconds + t_rhs
-    est = setup + per_cycle * cycles
-    # one V-cycle (max_fmg_iter 0) for comparison with the GPU's V-cycles
-    _, repv, _ = O.solve(C, bt, rhs, dx, fixed_iter=1, max_fmg_iter=0)
-    v_cycle = repv.seconds - repv.setup_seconds
-    # one operator application at full size, median of ten
-    fap = []
-    for _ in range(10):
-        t3 = time.perf_counter()
-        O.fapply(C, bt, x, dx)
-        fap.append(time.perf_counter() - t3)
-    return {"value": est, "unit": "s", "cores": threads, "kind": "port",
-            "sample": "oracle (C++ restatement of the reference CPU path, OpenMP) on %d host threads: RHS build + "
-                      "set-up + %d fixed FP64 F-cycles at the full %d^3 size; solve time = set-up + "
-                      "per-cycle time x %d cycles (the FP64 F-cycle count of this input to 1e-8)"
-                      % (threads, sample_cycles, n, cycles),
-            "per_cycle_s": per_cycle, "v_cycle_s": v_cycle, "setup_s": setup, "fapply_s": float(np.median(fap)),
-            "fapply_node_updates_per_s": float(n ** 3 / np.median(fap)), "sample_wall_s": time.perf_counter() - t0}
+    x, rep, hist = O.solve(C, bt, rhs, dx, tol_rel=TOL)
+    seconds = time.perf_counter() - t0
+    info = {"seconds": seconds, "rhs_s": t_rhs, "setup_s": rep.setup_seconds, "f_cycles": rep.iters,
+            "status": rep.status, "final_rel_resnorm": rep.final_resnorm / rep.rhsnorm0}
+    xr = None
+    if refine:
+        t1 = time.perf_counter()
+        xr, rep2, _ = O.solve(C, bt, rhs, dx, tol_rel=ORACLE_TOL, x0=x, max_iter=200)
+        info["refined"] = {"tol_rel": ORACLE_TOL, "extra_f_cycles": rep2.iters, "status": rep2.status,
+                           "final_rel_resnorm": rep2.final_resnorm / rep.rhsnorm0,
+                           "seconds": time.perf_counter() - t1}
+    return x, xr, info
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU path (oracle restatement) on
+    all host cores, whole FP64 solves of the same workload; rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    name, n, C, F0, bc, dx = workload(args.config, args.n)
+    O, threads = load_oracle()
+    bt, _ = bc.tables()
+    # warm-up: full-size operator applications (threads started, pages touched)
+    z = np.zeros((3, n, n, n))
+    for _ in range(args.warmup):
+        O.fapply(C, bt, z, dx)
+    times, infos = [], []
+    t_start = time.perf_counter()
+    while len(times) < args.steps:
+        _, _, info = oracle_solve(O, C, F0, bc, dx, refine=False)
+        times.append(info["seconds"])
+        infos.append(info)
+        if time.perf_counter() - t_start + info["seconds"] > REF_BUDGET_S:
+            break
+    v = float(np.mean(times))
+    guess = bool(args.guess) and os.path.exists(args.guess)
+    cpu = {"value": v, "unit": "s", "cores": threads, "kind": "port",
+           "sample": "%d whole FP64 solve(s) to %g (RHS + set-up + %d F-cycles) of the full %d^3 workload by the "
+                     "oracle (C++ restatement of the reference CPU path, OpenMP) on %d host threads; warm-up: %d "
+                     "full-size Fapply calls" % (len(times), TOL, infos[-1]["f_cycles"], n, threads, args.warmup),
+           "solves": infos}
+    line = {"impl": "reference", "metric": metric_name(n, guess),
+            "value": v, "unit": "s", "n_gpus": args.gpus, "steps": len(times), "warmup": args.warmup,
+            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": config_dict(name, n, C),
+            "cpu_baseline": cpu, "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
 
 
 def metric_name(n, guess):
@@ -227,30 +288,130 @@ def reduce_max(x, dist, device):
     return float(t.item())
 
 
-def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
-    name, n, C, F0, bc, dx = workload(args.config, args.n)
-    cycles = FP64_CYCLES[args.config]
-    vals = []
-    for s in range(args.warmup + args.steps):
-        r = cpu_sample(args.config, args.n, C, F0, bc, dx, cycles)
-        if s >= args.warmup:
-            vals.append(r["value"])
-        if s == 0 and r["sample_wall_s"] * (args.warmup + args.steps) > 240:
-            # keep the whole run within minutes: the remaining steps reuse this sample
-            vals = [r["value"]] * args.steps
-            break
-    v = float(np.mean(vals))
-    r["value"] = v
-    guess = bool(args.guess) and os.path.exists(args.guess)
-    line = {"impl": "reference", "metric": metric_name(n, guess),
-            "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic", "config": {"workload": name, "nodes": n ** 3},
-            "cpu_baseline": r, "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
+# --------------------------------------------------------------- GPU helpers
+def fast_opts(A, n, args=None, smoother="jacobi"):
+    """The fast path's options: mixed FGMRES(V(1,1)), direct 5^3 bottom."""
+    pre = args.pre if args else 1
+    post = args.post if args else 1
+    kw = dict(precision=1, solver="fgmres", inner_tol=args.inner_tol if args else 1e-4,
+              krylov_dim=args.krylov if args else 20, bottom_solver="direct",
+              max_coarsening_level=max(nlevels(n) - 2, 0), pre_smooth=pre, post_smooth=post)
+    if smoother == "gs":
+        kw["smoother"] = 1
+    return A.default_opts(**kw)
+
+
+def timed_solve(A, torch, n, C, F0, bc, dx, opts, net=None, repeats=1, sym=None, tol=TOL):
+    """One Newton step (the linear solve from zero, or from the learned
+    guess) on device-resident inputs; host wall time of the synchronous
+    call, best of `repeats`.  Returns (u on the host, report, seconds)."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    sym = sym or ("isotropic" if C.shape[-1] == 2 else "majorminor")
+    op = A.Elastic(n, dx, sym, opts)
+    try:
+        op.SetBC(bc)
+        C_dev = torch.from_numpy(C).to(dev)
+        F0_dev = torch.from_numpy(F0).to(dev) if F0 is not None else None
+        F0keep = (A.DevicePtr(F0_dev.data_ptr()), 1) if F0_dev is not None else None
+        u = torch.zeros((3, n, n, n), dtype=torch.float64, device=dev)
+        b = torch.zeros_like(u)
+        torch.cuda.synchronize()
+        op.bc_init(A.DevicePtr(b.data_ptr()))
+        newton = A.Newton(op)
+        best, rep = None, None
+        for _ in range(repeats):
+            op.SetModel(A.DevicePtr(C_dev.data_ptr()))
+            u.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if net is not None:
+                rep = newton.solve_guess(net, A.DevicePtr(u.data_ptr()), A.DevicePtr(b.data_ptr()), F0keep,
+                                         tol_rel=tol, tol_abs=0.0, allow_not_converged=True)
+            else:
+                rep = newton.solve(A.DevicePtr(u.data_ptr()), A.DevicePtr(b.data_ptr()), F0keep, tol_rel=tol,
+                                   tol_abs=0.0, allow_not_converged=True)
+            torch.cuda.synchronize()
+            s = time.perf_counter() - t0
+            best = s if best is None else min(best, s)
+        return u.cpu().numpy(), rep, best
+    finally:
+        op.close()
+
+
+def rep_summary(rep, sec):
+    d = {"seconds": sec, "cycles": rep.get("iters"), "status": rep.get("status"),
+         "final_rel_resnorm": rep["final_resnorm"] / rep["rhsnorm0"] if rep.get("rhsnorm0") else None}
+    if "guess_used" in rep:
+        d["guess_used"] = rep["guess_used"]
+    return d
+
+
+def extra_configs(A, torch, net, O, args):
+    """Configs 1, 3, 4 and 5, each in minutes at most."""
+    from alamo_gb300 import bc as B
+    from alamo_gb300 import learn
+    out = {}
+    # config 1: 33^3 inclusion; Fapply on U[-1,1] against the oracle, and the
+    # FP64 V(2,2) V-cycle iteration to 1e-10 against the oracle's
+    name, n, C, F0, bc, dx = workload("c1")
+    bt, bv = bc.tables()
+    u = A.synth.uniform(A.synth.SEED_FAPPLY, (3, n, n, n))
+    with A.Elastic(n, dx, "isotropic") as op:
+        op.SetModel(np.ascontiguousarray(C))
+        op.SetBC(bc)
+        f = op.Fapply(u)
+    c1 = {"workload": name, "fapply_vs_oracle": rel_err(f, O.fapply(C, bt, u, dx)) if O else None}
+    o64 = A.default_opts(precision=0, max_fmg_iter=0)
+    x, rep, sec = timed_solve(A, torch, n, C, F0, bc, dx, o64, tol=1e-10)
+    c1["fp64_vcycles_to_1e-10"] = rep_summary(rep, sec)
+    if O:
+        b0 = O.bc_init(np.zeros((3, n, n, n)), bt, bv)
+        rhs = O.build_rhs(C, F0, bt, np.zeros((3, n, n, n)), b0, dx)
+        xo, rep_o, _ = O.solve(C, bt, rhs, dx, tol_rel=1e-10, max_fmg_iter=0)
+        c1["solution_vs_oracle_1e-10"] = rel_err(x, xo)
+    out["c1"] = c1
+    # config 3: 513^3 spheres, learned guess + mixed against plain FP64
+    # (the reference's F-cycles); error of the mixed solution against it
+    name, n, C, F0, bc, dx = workload("c3")
+    xm, repm, secm = timed_solve(A, torch, n, C, F0, bc, dx, fast_opts(A, n), net=net, repeats=2)
+    x64, rep64, sec64 = timed_solve(A, torch, n, C, F0, bc, dx, A.default_opts(precision=0))
+    out["c3"] = {"workload": name, "learned_mixed": rep_summary(repm, secm), "plain_fp64_fcycles": rep_summary(rep64, sec64),
+                 "speedup": sec64 / secm, "mixed_vs_fp64": rel_err(xm, x64),
+                 "timing": "host wall clock around one synchronous C-ABI call, device-resident inputs"}
+    del C, F0, xm, x64
+    # config 4: held-out learned-guess evaluation on the training
+    # distribution (inclusion media, zero-displacement faces)
+    if net is not None:
+        c4 = {}
+        for n, count in ((129, 6), (257, 3)):
+            rng = np.random.default_rng(1000003 + n)
+            rows = []
+            for _ in range(count):
+                C, F0, dx = learn.inclusion_medium(n, rng)
+                o = fast_opts(A, n)
+                x0, r0, s0 = timed_solve(A, torch, n, C, F0, B.Constant(), dx, o, repeats=2)
+                x1, r1, s1 = timed_solve(A, torch, n, C, F0, B.Constant(), dx, o, net=net, repeats=2)
+                rows.append({"zero": rep_summary(r0, s0), "guess": rep_summary(r1, s1),
+                             "guess_vs_zero_solution": rel_err(x1, x0)})
+            used = [r["guess"]["guess_used"] for r in rows]
+            c4["%d^3" % n] = {"seeds": count, "fallback_rate": 1.0 - float(np.mean(used)),
+                              "cycles_zero": float(np.mean([r["zero"]["cycles"] for r in rows])),
+                              "cycles_guess": float(np.mean([r["guess"]["cycles"] for r in rows])),
+                              "s_zero": float(np.mean([r["zero"]["seconds"] for r in rows])),
+                              "s_guess": float(np.mean([r["guess"]["seconds"] for r in rows])), "runs": rows}
+        out["c4"] = c4
+    # config 5: 256-grain polycrystal (out of the guess's distribution)
+    from alamo_gb300 import workloads as W
+    n = 257
+    C, dx = W.voronoi_cubic(n, 256, seed=5)
+    bc = B.TensionTest("uniaxial_stress_clamp", disp=0.01)
+    xm, repm, secm = timed_solve(A, torch, n, C, None, bc, dx, fast_opts(A, n), net=net, repeats=2)
+    x64, rep64, sec64 = timed_solve(A, torch, n, C, None, bc, dx, A.default_opts(precision=0))
+    out["c5"] = {"workload": "c5: 257^3 cubic Voronoi polycrystal, 256 grains, uniaxial_stress_clamp u_x=0.01",
+                 "learned_mixed": rep_summary(repm, secm), "plain_fp64_fcycles": rep_summary(rep64, sec64),
+                 "speedup": sec64 / secm, "mixed_vs_fp64": rel_err(xm, x64),
+                 "fallback_rate": None if net is None else float(not repm.get("guess_used", False))}
+    return out
 
 
 # --------------------------------------------------------------- GPU arm
@@ -259,7 +420,10 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    import ctypes
+
     import torch
+
     import alamo_gb300 as A
     from alamo_gb300 import _lib
 
@@ -283,21 +447,19 @@ def main():
     nc = C.shape[-1]
     sym = "isotropic" if nc == 2 else "majorminor"
     prec = 1 if args.precision == "mixed" else 0
-    nlev = 1
-    m = n
-    while (m - 1) % 2 == 0 and (m - 1) // 2 >= 2:
-        m = (m - 1) // 2 + 1
-        nlev += 1
     # the mixed FGMRES path runs V(1,1) as its preconditioner (fewer fine sweeps
-    # per Krylov step; 52 steps of V(1,1) beat 36 of V(2,2) at 257^3); the
+    # per Krylov step; 53 steps of V(1,1) beat 36 of V(2,2) at 257^3); the
     # FP64 arms keep the reference's V(2,2)
     pre, post = (args.pre, args.post) if prec else (2, 2)
-    opts = A.default_opts(precision=prec, inner_cycles=args.inner, solver=args.solver, inner_tol=args.inner_tol,
-                          krylov_dim=args.krylov, bottom_solver="direct", max_coarsening_level=max(nlev - 2, 0),
-                          pre_smooth=pre, post_smooth=post)
+    okw = dict(precision=prec, inner_cycles=args.inner, solver=args.solver, inner_tol=args.inner_tol,
+               krylov_dim=args.krylov, bottom_solver="direct", max_coarsening_level=max(nlevels(n) - 2, 0),
+               pre_smooth=pre, post_smooth=post)
+    if args.smoother == "gs":
+        okw["smoother"] = 1
+    opts = A.default_opts(**okw)
     op = A.Elastic(n, dx, sym, opts)
     stream = torch.cuda.Stream()
-    _lib.check(_lib.lib().agb_elastic_set_stream(op.h, __import__("ctypes").c_void_p(stream.cuda_stream)))
+    _lib.check(_lib.lib().agb_elastic_set_stream(op.h, ctypes.c_void_p(stream.cuda_stream)))
     op.SetBC(bc)
     dev = torch.device("cuda", local)
     C_dev = torch.from_numpy(C).to(dev)
@@ -317,20 +479,19 @@ def main():
         net = learn.UNet(65)
         net.load(args.guess)
 
-
     def step():
         op.SetModel(P(C_dev.data_ptr()))
         if net is not None:
             # learned initial guess with its residual-based fallback (zero
             # when the fallback fires) as the first iterate of the Newton
             # step's linear solve, in one call
-            r = newton.solve_guess(net, P(u_dev.data_ptr()), P(b_dev.data_ptr()), F0arg, tol_rel=1e-8, tol_abs=0.0)
+            r = newton.solve_guess(net, P(u_dev.data_ptr()), P(b_dev.data_ptr()), F0arg, tol_rel=TOL, tol_abs=0.0)
             guesses.append({"used": r["guess_used"]})
             reports.append(r)
         else:
             with torch.cuda.stream(stream):
                 u_dev.zero_()
-            reports.append(newton.solve(P(u_dev.data_ptr()), P(b_dev.data_ptr()), F0arg, tol_rel=1e-8,
+            reports.append(newton.solve(P(u_dev.data_ptr()), P(b_dev.data_ptr()), F0arg, tol_rel=TOL,
                                         tol_abs=0.0))
 
     for _ in range(args.warmup):
@@ -354,6 +515,7 @@ def main():
     fam = {k: op.profile_get(v) for k, v in FAMILY.items()}
     op.profile(False)
     sec = reduce_max(sec, dist, dev)
+    u_fast = u_dev.cpu().numpy()
 
     # dominant fine-level kernel and its roofline
     peaks, peak_kind = measured_peaks()
@@ -365,7 +527,7 @@ def main():
         per_launch_s = ms / cnt / 1e3
         alg_bytes = BYTES_PER_NODE[dom][nc] * N
         achieved = alg_bytes / per_launch_s / 1e9
-        traf = TRAFFIC_PER_NODE.get((dom, nc))
+        traf = TRAFFIC_PER_NODE.get((dom, nc)) if args.smoother == "jacobi" else None
         nb = N - (n - 2) ** 3  # boundary nodes
         roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"],
@@ -384,23 +546,20 @@ def main():
         u_h = torch.zeros_like(b_h).pin_memory()
         F0_h = torch.from_numpy(F0).pin_memory() if F0 is not None else None
 
-
         def step_host():
             op.SetModel(C_h.numpy())
             F0x = F0_h.numpy() if F0_h is not None else None
             if net is not None:
-                newton.solve_guess(net, u_h.numpy(), b_h.numpy(), F0x, tol_rel=1e-8, tol_abs=0.0)
+                newton.solve_guess(net, u_h.numpy(), b_h.numpy(), F0x, tol_rel=TOL, tol_abs=0.0)
             else:
                 u_h.zero_()
-                newton.solve(u_h.numpy(), b_h.numpy(), F0x, tol_rel=1e-8, tol_abs=0.0)
+                newton.solve(u_h.numpy(), b_h.numpy(), F0x, tol_rel=TOL, tol_abs=0.0)
 
         step_host()
         barrier()
         t0 = time.perf_counter()
-        e0.record(stream)
         for _ in range(args.steps):
             step_host()
-        e1.record(stream)
         barrier()
         wall = (time.perf_counter() - t0) / args.steps
         wall = reduce_max(wall, dist, dev)
@@ -412,33 +571,28 @@ def main():
         e2e = {"value": wall, "unit": "s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "timing": "host wall clock around synchronous C-ABI calls"}
 
-    # plain FP64 solve of the same input with the reference's solver
-    # settings: MLMG iterations that are all F-cycles (max_fmg_iter
-    # 100000000), V(2,2) inside them, BiCGStab bottom
-    plain = None
+    # FP64 GPU solves of the same input: (1) the reference's solver
+    # settings (MLMG iterations that are all F-cycles, V(2,2), BiCGStab
+    # bottom, full coarsening); (2) FP64 FGMRES(V(1,1)) with the fast path's
+    # direct 5^3 bottom -- the solver without FP32
+    plain, fp64_fgmres, u64 = None, None, None
     if not args.no_plain:
-        op.SetOpts(A.default_opts(precision=0))
-        ts = []
         try:
-            for _ in range(2):
-                op.SetModel(P(C_dev.data_ptr()))
-                with torch.cuda.stream(stream):
-                    u_dev.zero_()
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                r = newton.solve(P(u_dev.data_ptr()), P(b_dev.data_ptr()), F0arg, tol_rel=1e-8, tol_abs=0.0)
-                torch.cuda.synchronize()
-                ts.append(time.perf_counter() - t0)
-            plain = {"seconds": min(ts), "cycles": r["iters"], "cycle": "F (max_fmg_iter 100000000)",
-                     "final_rel_resnorm": r["final_resnorm"] / r["rhsnorm0"]}
-            u64 = u_dev.clone()
+            u64, r, s = timed_solve(A, torch, n, C, F0, bc, dx, A.default_opts(precision=0))
+            plain = rep_summary(r, s)
+            plain["cycle"] = "F (max_fmg_iter 100000000), V(2,2), BiCGStab bottom, full coarsening"
         except A.AgbError as e:
             plain = {"error": str(e)}
-        op.SetOpts(opts)
-        if "error" not in plain:
-            step()
-            diff = (u_dev - u64).abs().max().item() / u64.abs().max().item()
-            plain["mixed_vs_fp64_solution_rel_inf"] = diff
+        try:
+            o = A.default_opts(precision=0, solver="fgmres", krylov_dim=args.krylov, bottom_solver="direct",
+                               max_coarsening_level=max(nlevels(n) - 2, 0), pre_smooth=1, post_smooth=1)
+            u64g, r, s = timed_solve(A, torch, n, C, F0, bc, dx, o, repeats=2)
+            fp64_fgmres = rep_summary(r, s)
+            fp64_fgmres["cycle"] = "FP64 FGMRES(%d) preconditioned by V(1,1), direct 5^3 bottom" % args.krylov
+            fp64_fgmres["fast_path_speedup"] = s / sec
+            del u64g
+        except A.AgbError as e:
+            fp64_fgmres = {"error": str(e)}
 
     # Fapply throughput (fine level, FP64 and FP32), 20 launches each
     op.SetModel(P(C_dev.data_ptr()))
@@ -451,8 +605,8 @@ def main():
     x32, f32 = x_dev.float(), torch.empty_like(x_dev, dtype=torch.float32)
     torch.cuda.synchronize()
     for _ in range(20):
-        _lib.check(_lib.lib().agb_elastic_fapply_f32(op.h, 0, __import__("ctypes").c_void_p(x32.data_ptr()),
-                                                     __import__("ctypes").c_void_p(f32.data_ptr()), 1))
+        _lib.check(_lib.lib().agb_elastic_fapply_f32(op.h, 0, ctypes.c_void_p(x32.data_ptr()),
+                                                     ctypes.c_void_p(f32.data_ptr()), 1))
     fap = {}
     for key, famid in [("fp64", FAMILY["fapply_f64"]), ("fp32", FAMILY["fapply_f32"])]:
         cnt, ms = op.profile_get(famid)
@@ -461,11 +615,40 @@ def main():
         fap[key] = {"node_updates_per_s": N / per, "hbm_gbs": bpn * N / per / 1e9, "ms": per * 1e3,
                     "frac_of_hbm_peak": bpn * N / per / 1e9 / peaks["hbm_gbs"]}
     op.profile(False)
+    del f_dev, x_dev, x32, f32
 
-    cpu = None
+    # the oracle: CPU baseline (one whole solve to 1e-8) and the FP64
+    # solution (continued to 1e-12) the GPU results are measured against
+    cpu, oracle_err, O = None, None, None
     if rank == 0 and not args.no_cpu:
-        cycles = plain["cycles"] if plain and "cycles" in plain else FP64_CYCLES[args.config]
-        cpu = cpu_sample(args.config, args.n, C, F0, bc, dx, cycles)
+        O, threads = load_oracle()
+        xo8, xo12, info = oracle_solve(O, C, F0, bc, dx, refine=True)
+        bt, _ = bc.tables()
+        fap_t = []
+        for _ in range(5):
+            t3 = time.perf_counter()
+            O.fapply(C, bt, xo8, dx)
+            fap_t.append(time.perf_counter() - t3)
+        cpu = {"value": info["seconds"], "unit": "s", "cores": threads, "kind": "port",
+               "sample": "one whole FP64 solve to %g (RHS + set-up + %d F-cycles) of the full %d^3 workload by the "
+                         "oracle (C++ restatement of the reference CPU path, OpenMP) on %d host threads"
+                         % (TOL, info["f_cycles"], n, threads),
+               "solve": info, "fapply_s": float(np.median(fap_t)),
+               "fapply_node_updates_per_s": float(N / np.median(fap_t))}
+        ref = xo12 if xo12 is not None else xo8
+        oracle_err = {"reference": "oracle FP64 solve continued to %g" % ORACLE_TOL,
+                      "fast_path": rel_err(u_fast, ref),
+                      "oracle_at_1e-8": rel_err(xo8, ref)}
+        if u64 is not None:
+            oracle_err["plain_fp64_gpu"] = rel_err(u64, ref)
+        del xo8, xo12, ref
+
+    extra = None
+    op.close()
+    del C_dev, F0_dev, u_dev, b_dev
+    torch.cuda.empty_cache()
+    if rank == 0 and not args.no_extra and args.config == "c2" and not args.n:
+        extra = extra_configs(A, torch, net, O, args)
 
     rep = reports[-1] if reports else {}
     line = {
@@ -473,12 +656,15 @@ def main():
         "value": sec, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-cycle/f64-refinement" if prec else "f64", "data": "synthetic",
-        "config": {"workload": name, "nodes": N, "precision": args.precision, "solver": args.solver,
-                   "inner_tol": args.inner_tol, "krylov_dim": args.krylov, "bottom": "direct 5^3",
-                   "smoothing": "V(%d,%d), 2 damped-Jacobi sweeps per Fsmooth call" % (pre, post),
-                   "parallelism": "replicas" if world > 1 else "single-gpu",
-                   "l2": "inputs larger than L2 (%.1f GB of stiffness)" % (C.nbytes / 1e9)},
+        "config": config_dict(name, n, C),
+        "gpu_solver": {"precision": args.precision, "solver": args.solver, "inner_tol": args.inner_tol,
+                       "krylov_dim": args.krylov, "bottom": "direct 5^3",
+                       "smoothing": "V(%d,%d), %s" % (pre, post, "2 damped-Jacobi sweeps per Fsmooth call"
+                                                      if args.smoother == "jacobi" else
+                                                      "multicolour Gauss-Seidel sweeps"),
+                       "parallelism": "replicas" if world > 1 else "single-gpu"},
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": ck,
+        "error_vs_fp64_oracle": oracle_err,
         "guess": ({"weights": os.path.relpath(args.guess, ROOT), "network_grid": 65,
                    "used_fraction": float(np.mean([g["used"] for g in guesses])) if guesses else None}
                   if net is not None else None),
@@ -486,13 +672,14 @@ def main():
                   "final_rel_resnorm_l2": (rep.get("final_resnorm_l2", 0) / rep["rhsnorm_l2"]) if rep else None,
                   "final_rel_resnorm": (rep.get("final_resnorm", 0) / rep["rhsnorm0"]) if rep else None,
                   "levels": rep.get("nlevels")},
-        "plain_fp64": plain,
+        "plain_fp64": plain, "fp64_fgmres": fp64_fgmres,
         "speedup_vs_plain_fp64": (plain["seconds"] / sec) if plain and "seconds" in plain else None,
-        "fapply": fap, "kernels_in_timed_region": kernels,
+        "fapply": fap, "kernels_in_timed_region": kernels, "other_configs": extra,
     }
     if rank == 0:
         print(json.dumps(line))
-    op.close()
+    if net is not None:
+        net.close()
     if dist is not None:
         dist.destroy_process_group()
 

@@ -93,8 +93,8 @@ typedef struct agb_solver_opts {
     int krylov_dim;           /* FGMRES: basis size per cycle, <= 39 (20) */
     double inner_tol;         /* mixed FGMRES: residual reduction of one FP32 inner solve (1e-4) */
     int bottom_solver;        /* agb_bottom_solver (AGB_BOTTOM_BICGSTAB) */
-    int fine_kernel;          /* FP32 fine-level stencil kernels: 0 z-marching with TMA-staged stiffness
-                                 (default), 1 one thread per node, 2 z-marching with register-staged stiffness */
+    int fine_kernel;          /* FP32 stencil kernels: 0 z-marching with TMA-staged stiffness on the
+                                 levels that allow it (default), 1 one thread per node everywhere */
     int krylov_reorth;        /* FGMRES Gram-Schmidt: 1 re-orthogonalise once, 0 single pass (default) */
     int tma_min_nodes;        /* FP32 levels with at least this many nodes use the z-marching kernels
                                  (fine_kernel 0); smaller ones the per-node kernels (0: 30000) */
@@ -183,6 +183,14 @@ agb_status agb_elastic_fsmooth(agb_elastic* h, int level, double* x, const doubl
  * receives {||r||_inf, ||r||_2}. */
 agb_status agb_elastic_residual(agb_elastic* h, int level, const double* x, const double* b, double* r,
                                 double norms[2], int where);
+/* The FP32 forms of Fsmooth and the residual that the mixed-precision cycles
+ * run (the z-marching TMA-staged kernels on the levels large enough for
+ * them, the per-node kernels elsewhere), on the level's FP32 stiffness:
+ * x <- ncalls x 2 damped-Jacobi sweeps (the same update as
+ * agb_elastic_fsmooth, evaluated as x + w (b - Ax) / D); r = b - A x.
+ * x, b, r: 3*N floats of that level. */
+agb_status agb_elastic_fsmooth_f32(agb_elastic* h, int level, float* x, const float* b, int ncalls, int where);
+agb_status agb_elastic_residual_f32(agb_elastic* h, int level, const float* x, const float* b, float* r, int where);
 /* Operator<Grid::Node>::restriction (src/Operator/Operator.cpp:262-363):
  * fine field of level crse_level-1 -> coarse field of level crse_level */
 agb_status agb_elastic_restrict(agb_elastic* h, int crse_level, const double* fine, double* crse, int where);
@@ -254,21 +262,24 @@ agb_status agb_newton_solve_neohookean(agb_elastic* h, const double* model, doub
 agb_status agb_elastic_tensor(agb_elastic* h, const double* u, int which, int voigt, double* out, int where);
 
 /* ------------------------------------------------ allocation-free call */
-/* No counterpart in the reference.  For callers that cannot call cudaMalloc
- * (inside a CUDA graph capture, inside another library's memory pool, or in
- * a host code that reserves the device up front): r = b - A x and its norms
- * {||r||_inf, ||r||_2} with no allocation and no handle.  The caller passes
- * device arrays only: C_soa is the per-node stiffness split per component
- * (2 or 21 arrays of nx*ny*nz doubles one after another), bc_type the 26*3
- * table of agb_elastic_set_bc, x, b, r vector fields (3*N doubles); norms is
- * host memory.  The per-block partial norms live in a fixed 2 MiB device
- * array inside the library (AGB_NOALLOC_MAX_BLOCKS pairs of doubles, one per
- * 32x4x2-node block, held by every GPU that loads the library until exit), so
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * a host code whose memory arena took the whole device at start-up, a plugin
+ * living inside such a code, or a time-stepping loop that must not call
+ * cudaMalloc/cudaFree between steps because they can synchronise the device.
+ * r = b - A x and its norms {||r||_inf, ||r||_2} with no allocation and no
+ * handle.  Device memory: C_soa, the per-node stiffness split per component
+ * (2 or 21 arrays of nx*ny*nz doubles one after another), and the vector
+ * fields x, b, r (3*N doubles).  Host memory: dx, bc_type (the 26*3 table of
+ * agb_elastic_set_bc, read on the host before the launch) and norms.  The
+ * per-block partial norms live in a fixed 2 MiB device array inside the
+ * library (AGB_NOALLOC_MAX_BLOCKS pairs of doubles, one per block of the
+ * residual kernel, held by every GPU that loads the library until exit), so
  * grids of more than AGB_NOALLOC_MAX_BLOCKS blocks (about 33.5M nodes) return
- * AGB_LIMIT.  The first call on a device looks the array's address up and
- * must come before any stream capture on that device.  Calls share the
- * array: calls that overlap on the GPU race and give wrong norms.  Runs on
- * `stream` (NULL: the legacy default stream) and returns after it. */
+ * AGB_LIMIT.  The first call on a device looks the array's address up (do it
+ * before any stream capture on that device) and caches it; a device reset
+ * after that call is not supported.  Calls share the array: calls that
+ * overlap on the GPU race and give wrong norms.  Runs on `stream` (NULL: the
+ * legacy default stream) and returns after it. */
 #define AGB_NOALLOC_MAX_BLOCKS 131072
 agb_status agb_residual_norms_noalloc(int nx, int ny, int nz, const double dx[3], int sym, const double* C_soa,
                                       const int* bc_type, const double* x, const double* b, double* r,

@@ -59,26 +59,44 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--gpus", "2"])
     args = bench.parse()
     called = []
-    monkeypatch.setattr(bench, "cpu_sample", lambda *a, **k: called.append(1))
+    monkeypatch.setattr(bench, "oracle_solve", lambda *a, **k: called.append(1))
+    monkeypatch.setattr(bench, "load_oracle", lambda: called.append(1))
     bench.run_reference(args)
     assert not called
     assert capsys.readouterr().out == ""
 
 
 def test_reference_arm_prints_the_gpu_arms_metric(monkeypatch, capsys):
-    """Rank 0's reference line carries the metric string the GPU arm prints
-    for the same workload (the sample itself is stubbed out)."""
+    """Rank 0's reference line carries the metric string and the config the
+    GPU arm prints for the same workload (the solve itself is stubbed out);
+    it reports the whole solves it timed as its steps."""
     import json
+    import numpy as np
     sys.path.insert(0, ROOT)
     import bench
     monkeypatch.setenv("RANK", "0")
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "2", "--warmup", "1"])
     args = bench.parse()
-    monkeypatch.setattr(bench, "workload", lambda cfg, n=0: ("tiny", 5, None, None, None, 0.25))
-    monkeypatch.setattr(bench, "cpu_sample", lambda *a, **k: {"value": 2.0, "sample_wall_s": 0.01})
+    C = np.zeros((5, 5, 5, 21))
+
+    class _O:
+        @staticmethod
+        def fapply(*a):
+            return None
+
+    class _BC:
+        @staticmethod
+        def tables():
+            return None, None
+
+    monkeypatch.setattr(bench, "workload", lambda cfg, n=0: ("tiny", 5, C, None, _BC(), 0.25))
+    monkeypatch.setattr(bench, "load_oracle", lambda: (_O(), 4))
+    monkeypatch.setattr(bench, "oracle_solve", lambda *a, **k: (None, None, {"seconds": 2.0, "f_cycles": 7}))
     bench.run_reference(args)
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     guess = bool(args.guess) and os.path.exists(args.guess)
     assert line["impl"] == "reference"
     assert line["metric"] == bench.metric_name(5, guess)
+    assert line["config"] == bench.config_dict("tiny", 5, C)
+    assert line["steps"] == 2 and line["warmup"] == 1
     assert line["value"] == 2.0 and line["e2e"]["value"] == 2.0

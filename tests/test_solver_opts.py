@@ -39,7 +39,7 @@ def test_parse_rejects(agb, kv, err):
 @pytest.mark.parametrize("field,value", [
     ("pre_smooth", -1), ("post_smooth", -1), ("final_smooth", -1), ("bottom_smooth", -1),
     ("bottom_max_iter", -1), ("max_iter", -1), ("omega", 0.0), ("omega", 2.5), ("precision", 5),
-    ("solver", 3), ("bottom_solver", 7), ("fine_kernel", 3), ("tma_min_nodes", -1)])
+    ("solver", 3), ("bottom_solver", 7), ("fine_kernel", 2), ("tma_min_nodes", -1)])
 def test_create_rejects_bad_options(agb, field, value):
     """agb_elastic_create checks the options before it touches the GPU and
     answers AGB_BAD_ARG with a message naming the problem."""

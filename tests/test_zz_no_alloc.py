@@ -1,8 +1,9 @@
 """The allocation-free residual entry point, for callers that cannot call
-cudaMalloc (a CUDA graph capture in progress, a host code that owns the whole
-device memory, another library's pool): it must give what the ordinary
-residual entry point gives, call after call, while using only the caller's
-arrays and the library's fixed device scratch.
+cudaMalloc (a host code whose memory arena took the whole device, a plugin
+inside one, a step loop that must not synchronise the device through
+cudaMalloc/cudaFree): it must give what the ordinary residual entry point
+and the oracle give, call after call, while using only the caller's arrays
+and the library's fixed device scratch.
 
 This file is collected last on purpose, so a run that stops at the first
 failure has already run every other test.
@@ -33,7 +34,7 @@ def test_noalloc_rejects_oversized_grid(agb):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", ["c1", "voronoi"])
-def test_noalloc_matches_residual_entry_point(agb, case):
+def test_noalloc_matches_residual_entry_point(agb, oracle, case):
     torch = pytest.importorskip("torch")
     from alamo_gb300 import _lib
     if case == "c1":
@@ -64,4 +65,9 @@ def test_noalloc_matches_residual_entry_point(agb, case):
         assert np.abs(rr - r_ref).max() <= 1e-12 * np.abs(r_ref).max()
         assert abs(norms[0] - inf_ref) <= 1e-12 * inf_ref
         assert abs(norms[1] - l2_ref) <= 1e-12 * l2_ref
+        # and the oracle's residual (Operator.cpp:635-657) on the same inputs
+        r_orc = oracle.residual(C, bt, x.cpu().numpy(), b.cpu().numpy(), dx)
+        assert np.abs(rr - r_orc).max() <= 1e-12 * np.abs(r_orc).max()
+        assert abs(norms[0] - np.abs(r_orc).max()) <= 1e-12 * np.abs(r_orc).max()
+        assert abs(norms[1] - np.sqrt((r_orc ** 2).sum())) <= 1e-12 * np.sqrt((r_orc ** 2).sum())
     op.close()
