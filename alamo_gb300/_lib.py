@@ -34,6 +34,7 @@ SYM_ISOTROPIC, SYM_MAJORMINOR, SYM_MAJOR = 0, 1, 2
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 SOLVER_VCYCLE, SOLVER_FGMRES = 0, 1
 BOTTOM_BICGSTAB, BOTTOM_DIRECT, BOTTOM_SMOOTHER = 0, 1, 2
+SMOOTHER_JACOBI, SMOOTHER_GS = 0, 1
 K_FAPPLY_F64, K_JACOBI_F64, K_RESIDUAL_F64, K_FAPPLY_F32, K_JACOBI_F32, K_RESIDUAL_F32, K_RESTRICT, K_PROLONG, \
     K_BOTTOM = range(9)
 
@@ -63,6 +64,7 @@ class SolverOpts(ctypes.Structure):
         ("krylov_reorth", ctypes.c_int),
         ("tma_min_nodes", ctypes.c_int),
         ("max_fmg_iter", ctypes.c_int),
+        ("smoother", ctypes.c_int),
     ]
 
 

@@ -18,6 +18,10 @@ cudaError_t launch_fapply(int sym, const T* u, const T* C, const LevelGeom<T>& G
 // diag of A (Operator::Elastic::Diagonal)
 template <typename T>
 cudaError_t launch_diagonal(int sym, const T* C, const LevelGeom<T>& G, const BcTable& bc, T* diag, cudaStream_t s);
+// one colour (0..7) of the multicolour Gauss-Seidel sweep, in place on x
+template <typename T>
+cudaError_t launch_gs_colour(int sym, T* x, const T* b, const T* diag, const T* C, const LevelGeom<T>& G,
+                             const BcTable& bc, T omega_b, int colour, cudaStream_t s);
 // One damped-Jacobi sweep fused with the operator:
 //   xout = (1-w) x + w (b - (A x - diag x)) / diag     (x == nullptr: x = 0)
 template <typename T>

@@ -69,7 +69,7 @@ struct Lev {
     // FP32 levels swept by the TMA stencil kernels: stiffness with the x
     // pitch padded to 4 values and its tensor map
     T* Cpad = nullptr;
-    CUtensorMap map{};
+    ZtMaps map{};
     bool tma = false;
     // psi of this level (ghosted, LevelGeom::psi layout), owned; the FP64
     // fine level uses the handle's psi_fine instead
@@ -397,7 +397,7 @@ agb_status build_f32(agb_elastic* h) {
         CK(launch_recip(v.diag, v.dinv, 3 * G.N, h->stream));
         h->launches += 2;
         if (!v.tma) {
-            CK(make_stiffness_map(v.Cpad, G.nx, G.ny, G.nz, h->nc, &v.map));
+            CK(make_stiffness_maps(v.Cpad, G.nx, G.ny, G.nz, h->nc, &v.map));
             v.tma = true;
         }
     }
@@ -534,6 +534,17 @@ agb_status smooth(agb_elastic* h, std::vector<Lev<T>>& L, int l, int ncalls, boo
         CK(cudaMemsetAsync(v.cor, 0, sizeof(T) * 3 * v.G.N, h->stream));
         return AGB_OK;
     }
+    if (h->opts.smoother == AGB_SMOOTHER_GS) {
+        // multicolour Gauss-Seidel: in place on cor, eight colours per sweep
+        if (cor_zero) CK(cudaMemsetAsync(v.cor, 0, sizeof(T) * 3 * v.G.N, h->stream));
+        for (int s = 0; s < sweeps; s++) {
+            ProfScope ps(h, Fam<T>::J, l == 0);
+            for (int c = 0; c < 8; c++)
+                CK(launch_gs_colour<T>(h->sym, v.cor, v.res, v.diag, v.C, v.G, h->bc, w, c, h->stream));
+            h->launches += 8;
+        }
+        return AGB_OK;
+    }
     for (int s = 0; s < sweeps; s++) {
         if (s == 0 && cor_zero && first_done) {
             // the sweep from zero was written into tmp by the restriction
@@ -601,7 +612,7 @@ agb_status vcycle(agb_elastic* h, std::vector<Lev<T>>& L, int l0 = 0) {
     if (l0 == nl - 1) return bottom<T>(h, L);
     // levels below l0 receive their first pre-smoothing sweep (from a zero
     // correction) from the restriction that fills their right-hand side
-    const bool fuse = h->opts.pre_smooth > 0;
+    const bool fuse = h->opts.pre_smooth > 0 && h->opts.smoother == AGB_SMOOTHER_JACOBI;
     for (int l = l0; l < nl - 1; l++) {
         Lev<T>& v = L[l];
         TRY(smooth<T>(h, L, l, h->opts.pre_smooth, true, fuse && l > l0));
@@ -1051,6 +1062,7 @@ agb_status agb_default_opts(agb_solver_opts* o) {
     o->krylov_reorth = 0;
     o->tma_min_nodes = 0;
     o->max_fmg_iter = 100000000;
+    o->smoother = AGB_SMOOTHER_JACOBI;
     return AGB_OK;
 }
 
@@ -1066,6 +1078,8 @@ static agb_status check_opts(const agb_solver_opts* o) {
         return fail(AGB_BAD_ARG, "unknown bottom solver");
     if (o->fine_kernel < 0 || o->fine_kernel > 1) return fail(AGB_BAD_ARG, "fine_kernel must be 0 or 1");
     if (o->tma_min_nodes < 0) return fail(AGB_BAD_ARG, "tma_min_nodes must be >= 0");
+    if (o->smoother != AGB_SMOOTHER_JACOBI && o->smoother != AGB_SMOOTHER_GS)
+        return fail(AGB_BAD_ARG, "unknown smoother");
     if (o->solver == AGB_SOLVER_FGMRES && (o->krylov_dim < 1 || o->krylov_dim > 39))
         return fail(AGB_BAD_ARG, "krylov_dim must lie in [1, 39]");
     if (o->solver == AGB_SOLVER_FGMRES && !(o->inner_tol > 0.0 && o->inner_tol < 1.0))

@@ -30,15 +30,18 @@ __device__ __forceinline__ double blk_sum(double v, double* sh) {
     for (int q = 0; q < (int)(blockDim.x >> 5); q++) r += sh[q];
     return r;
 }
+// max that keeps a NaN (fmax drops it): a NaN anywhere in the bottom
+// iteration must reach the breakdown test
+__device__ __forceinline__ double nan_max(double a, double b) { return a != a ? a : (b != b ? b : fmax(a, b)); }
 __device__ __forceinline__ double blk_max(double v, double* sh) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = nan_max(v, __shfl_xor_sync(0xffffffffu, v, o));
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     __syncthreads();
     if (l == 0) sh[w] = v;
     __syncthreads();
     double r = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); q++) r = fmax(r, sh[q]);
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) r = nan_max(r, sh[q]);
     return r;
 }
 
@@ -109,7 +112,7 @@ __global__ void __launch_bounds__(BOT_THREADS) k_bottom(const double* __restrict
     for (int64_t q = tid; q < n3; q += nt) {
         const double rv = rhs[q] / dg[q] - t[q];
         r[q] = rv; rh[q] = rv; so[q] = sol[q]; sol[q] = 0.0; p[q] = 0.0; v[q] = 0.0;
-        lm = fmax(lm, fabs(rv));
+        lm = nan_max(lm, fabs(rv));
     }
     const double rnorm0 = blk_max(lm, sh);
     double rnorm = rnorm0;
@@ -142,9 +145,10 @@ __global__ void __launch_bounds__(BOT_THREADS) k_bottom(const double* __restrict
             sol[q] += alpha * p[q];
             const double sv = r[q] - alpha * v[q];
             s[q] = sv;
-            lm = fmax(lm, fabs(sv));
+            lm = nan_max(lm, fabs(sv));
         }
         rnorm = blk_max(lm, sh);
+        if (rnorm != rnorm) { ret = 5; break; }
         if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
         bot_apply<SYM>(s, t, C, dg, G, bc);
         double ltt = 0.0, lts = 0.0;
@@ -158,9 +162,10 @@ __global__ void __launch_bounds__(BOT_THREADS) k_bottom(const double* __restrict
             sol[q] += omg * s[q];
             const double rv = s[q] - omg * t[q];
             r[q] = rv;
-            lm = fmax(lm, fabs(rv));
+            lm = nan_max(lm, fabs(rv));
         }
         rnorm = blk_max(lm, sh);
+        if (rnorm != rnorm) { ret = 5; break; }
         if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
         if (omg == 0.0) { ret = 4; break; }
         rho_1 = rho;

@@ -164,6 +164,57 @@ template cudaError_t launch_jacobi<double>(int, const double*, const double*, co
 template cudaError_t launch_jacobi<float>(int, const float*, const float*, const float*, const float*,
                                           const LevelGeom<float>&, const BcTable&, float, float*, cudaStream_t);
 
+// ---------------------------------------------------------------- Gauss-Seidel
+// One colour of the multicolour Gauss-Seidel sweep (no counterpart in the
+// reference, whose smoother is the damped Jacobi above).  Colour c =
+// (i & 1) + 2 (j & 1) + 4 (k & 1); a row reads u only at offsets in the
+// 19-point set (components in {-1, 0, 1}, at most two non-zero), so nodes of
+// one colour never read each other and x is updated in place.  One thread
+// per node of the colour: x_p += w (b_p - (A x)_p) / D_p, w = 1 on interior
+// rows and the Jacobi damping on boundary rows.
+template <typename T, int SYM, bool PSI>
+__global__ void __launch_bounds__(256) k_gs_colour(T* x, const T* __restrict__ b, const T* __restrict__ dg,
+                                                   const T* __restrict__ C, LevelGeom<T> G, BcTable bc,
+                                                   T omega_b, int colour) {
+    const int i = 2 * (blockIdx.x * BX + threadIdx.x) + (colour & 1);
+    const int j = 2 * (blockIdx.y * BY + threadIdx.y) + ((colour >> 1) & 1);
+    const int k = 2 * (blockIdx.z * BZ + threadIdx.z) + ((colour >> 2) & 1);
+    if (i >= G.nx || j >= G.ny || k >= G.nz) return;
+    const int64_t id = i + G.sy * j + G.sz * k;
+    T ax[3];
+    apply_node<T, SYM, PSI>(x, C, G, bc, i, j, k, id, ax);
+    const bool bnd = i == 0 || j == 0 || k == 0 || i == G.nx - 1 || j == G.ny - 1 || k == G.nz - 1;
+    const T w = bnd ? omega_b : T(1);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const int64_t q = c * G.N + id;
+        x[q] = x[q] + w * (b[q] - ax[c]) / dg[q];
+    }
+}
+
+template <typename T>
+cudaError_t launch_gs_colour(int sym, T* x, const T* b, const T* diag, const T* C, const LevelGeom<T>& G,
+                             const BcTable& bc, T omega_b, int colour, cudaStream_t s) {
+    const int hx = (G.nx - (colour & 1) + 1) / 2, hy = (G.ny - ((colour >> 1) & 1) + 1) / 2,
+              hz = (G.nz - ((colour >> 2) & 1) + 1) / 2;
+    if (hx <= 0 || hy <= 0 || hz <= 0) return cudaSuccess;
+    dim3 blk(BX, BY, BZ), grd = grid3(hx, hy, hz);
+    if (G.psi) {
+        if (sym == SYM_ISO) k_gs_colour<T, SYM_ISO, true><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega_b, colour);
+        else if (sym == SYM_MAJ) k_gs_colour<T, SYM_MAJ, true><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega_b, colour);
+        else k_gs_colour<T, SYM_MM, true><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega_b, colour);
+    } else {
+        if (sym == SYM_ISO) k_gs_colour<T, SYM_ISO, false><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega_b, colour);
+        else if (sym == SYM_MAJ) k_gs_colour<T, SYM_MAJ, false><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega_b, colour);
+        else k_gs_colour<T, SYM_MM, false><<<grd, blk, 0, s>>>(x, b, diag, C, G, bc, omega_b, colour);
+    }
+    return cudaGetLastError();
+}
+template cudaError_t launch_gs_colour<double>(int, double*, const double*, const double*, const double*,
+                                              const LevelGeom<double>&, const BcTable&, double, int, cudaStream_t);
+template cudaError_t launch_gs_colour<float>(int, float*, const float*, const float*, const float*,
+                                             const LevelGeom<float>&, const BcTable&, float, int, cudaStream_t);
+
 // ---------------------------------------------------------------- residual
 // Block reduction of (max, sum) pairs: warp shuffles, then one warp over the
 // per-warp results.  Deterministic for a fixed launch shape.

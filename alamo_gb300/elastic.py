@@ -49,10 +49,14 @@ def default_opts(**kw):
     o = L.SolverOpts()
     L.check(L.lib().agb_default_opts(ctypes.byref(o)))
     for k, v in kw.items():
+        if not hasattr(o, k):
+            raise TypeError("unknown solver option %r" % k)
         if k == "precision" and isinstance(v, str):
             v = {"fp64": L.PRECISION_FP64, "mixed": L.PRECISION_MIXED}[v]
         if k == "solver" and isinstance(v, str):
             v = {"vcycle": L.SOLVER_VCYCLE, "fgmres": L.SOLVER_FGMRES}[v]
+        if k == "smoother" and isinstance(v, str):
+            v = {"jacobi": L.SMOOTHER_JACOBI, "gs": L.SMOOTHER_GS}[v]
         if k == "bottom_solver" and isinstance(v, str):
             v = {"bicgstab": L.BOTTOM_BICGSTAB, "direct": L.BOTTOM_DIRECT, "smoother": L.BOTTOM_SMOOTHER}[v]
         setattr(o, k, v)

@@ -226,12 +226,17 @@ def oracle_solve(O, C, F0, bc, dx, refine=True):
     seconds = time.perf_counter() - t0
     info = {"seconds": seconds, "rhs_s": t_rhs, "setup_s": rep.setup_seconds, "f_cycles": rep.iters,
             "status": rep.status, "final_rel_resnorm": rep.final_resnorm / rep.rhsnorm0}
+    if rep.status != 0:
+        info["error"] = "the oracle's solve did not reach %g (status %d)" % (TOL, rep.status)
     xr = None
     if refine:
+        # continued with the exact 5^3 bottom (the reference's BiCGStab on
+        # the singular 3^3 bottom of the clamp stalls well above 1e-12)
         t1 = time.perf_counter()
-        xr, rep2, _ = O.solve(C, bt, rhs, dx, tol_rel=ORACLE_TOL, x0=x, max_iter=200)
+        xr, rep2, _ = O.solve(C, bt, rhs, dx, tol_rel=ORACLE_TOL, x0=x, max_iter=100, bottom_solver=1,
+                              max_coarsening_level=max(nlevels(n) - 2, 0))
         info["refined"] = {"tol_rel": ORACLE_TOL, "extra_f_cycles": rep2.iters, "status": rep2.status,
-                           "final_rel_resnorm": rep2.final_resnorm / rep.rhsnorm0,
+                           "bottom": "direct 5^3", "final_rel_resnorm": rep2.final_resnorm / rep.rhsnorm0,
                            "seconds": time.perf_counter() - t1}
     return x, xr, info
 
@@ -346,43 +351,80 @@ def rep_summary(rep, sec):
     return d
 
 
+def fp64_fgmres_opts(A, n, krylov=20):
+    """FP64 FGMRES(V(1,1)) with the fast path's direct 5^3 bottom."""
+    return A.default_opts(precision=0, solver="fgmres", krylov_dim=krylov, bottom_solver="direct",
+                          max_coarsening_level=max(nlevels(n) - 2, 0), pre_smooth=1, post_smooth=1)
+
+
+def guarded(fn):
+    """Run one extra measurement; a failure is recorded, not raised."""
+    try:
+        return fn()
+    except Exception as e:  # noqa: BLE001 -- reported in the line
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
+def compare_fp64(A, torch, n, C, F0, bc, dx, net, name):
+    """Learned guess + mixed against the FP64 solves of the same input: the
+    reference's settings (F-cycles, BiCGStab bottom) and FP64 FGMRES with the
+    direct bottom; the mixed solution's error against the latter."""
+    xm, repm, secm = timed_solve(A, torch, n, C, F0, bc, dx, fast_opts(A, n), net=net, repeats=2)
+    out = {"workload": name, "learned_mixed": rep_summary(repm, secm),
+           "timing": "host wall clock around one synchronous C-ABI call, device-resident inputs"}
+    x64, rep64, sec64 = timed_solve(A, torch, n, C, F0, bc, dx, fp64_fgmres_opts(A, n))
+    out["fp64_fgmres_direct_bottom"] = rep_summary(rep64, sec64)
+    out["mixed_vs_fp64"] = rel_err(xm, x64)
+    del xm, x64
+
+    def ref_settings():
+        _, rep, sec = timed_solve(A, torch, n, C, F0, bc, dx, A.default_opts(precision=0))
+        d = rep_summary(rep, sec)
+        d["speedup_of_learned_mixed"] = sec / secm
+        return d
+    out["plain_fp64_fcycles"] = guarded(ref_settings)
+    if net is not None:
+        out["fallback_rate"] = float(not repm.get("guess_used", False))
+    return out
+
+
 def extra_configs(A, torch, net, O, args):
     """Configs 1, 3, 4 and 5, each in minutes at most."""
     from alamo_gb300 import bc as B
     from alamo_gb300 import learn
+    from alamo_gb300 import workloads as W
     out = {}
-    # config 1: 33^3 inclusion; Fapply on U[-1,1] against the oracle, and the
-    # FP64 V(2,2) V-cycle iteration to 1e-10 against the oracle's
-    name, n, C, F0, bc, dx = workload("c1")
-    bt, bv = bc.tables()
-    u = A.synth.uniform(A.synth.SEED_FAPPLY, (3, n, n, n))
-    with A.Elastic(n, dx, "isotropic") as op:
-        op.SetModel(np.ascontiguousarray(C))
-        op.SetBC(bc)
-        f = op.Fapply(u)
-    c1 = {"workload": name, "fapply_vs_oracle": rel_err(f, O.fapply(C, bt, u, dx)) if O else None}
-    o64 = A.default_opts(precision=0, max_fmg_iter=0)
-    x, rep, sec = timed_solve(A, torch, n, C, F0, bc, dx, o64, tol=1e-10)
-    c1["fp64_vcycles_to_1e-10"] = rep_summary(rep, sec)
-    if O:
-        b0 = O.bc_init(np.zeros((3, n, n, n)), bt, bv)
-        rhs = O.build_rhs(C, F0, bt, np.zeros((3, n, n, n)), b0, dx)
-        xo, rep_o, _ = O.solve(C, bt, rhs, dx, tol_rel=1e-10, max_fmg_iter=0)
-        c1["solution_vs_oracle_1e-10"] = rel_err(x, xo)
-    out["c1"] = c1
-    # config 3: 513^3 spheres, learned guess + mixed against plain FP64
-    # (the reference's F-cycles); error of the mixed solution against it
-    name, n, C, F0, bc, dx = workload("c3")
-    xm, repm, secm = timed_solve(A, torch, n, C, F0, bc, dx, fast_opts(A, n), net=net, repeats=2)
-    x64, rep64, sec64 = timed_solve(A, torch, n, C, F0, bc, dx, A.default_opts(precision=0))
-    out["c3"] = {"workload": name, "learned_mixed": rep_summary(repm, secm), "plain_fp64_fcycles": rep_summary(rep64, sec64),
-                 "speedup": sec64 / secm, "mixed_vs_fp64": rel_err(xm, x64),
-                 "timing": "host wall clock around one synchronous C-ABI call, device-resident inputs"}
-    del C, F0, xm, x64
-    # config 4: held-out learned-guess evaluation on the training
-    # distribution (inclusion media, zero-displacement faces)
-    if net is not None:
-        c4 = {}
+
+    def c1():
+        # 33^3 inclusion: Fapply on U[-1,1] against the oracle, and the FP64
+        # V(2,2) V-cycle iteration to 1e-10 against the oracle's
+        name, n, C, F0, bc, dx = workload("c1")
+        bt, bv = bc.tables()
+        u = A.synth.uniform(A.synth.SEED_FAPPLY, (3, n, n, n))
+        with A.Elastic(n, dx, "isotropic") as op:
+            op.SetModel(np.ascontiguousarray(C))
+            op.SetBC(bc)
+            f = op.Fapply(u)
+        d = {"workload": name, "fapply_vs_oracle": rel_err(f, O.fapply(C, bt, u, dx)) if O else None}
+        x, rep, sec = timed_solve(A, torch, n, C, F0, bc, dx, A.default_opts(precision=0, max_fmg_iter=0), tol=1e-10)
+        d["fp64_vcycles_to_1e-10"] = rep_summary(rep, sec)
+        if O:
+            b0 = O.bc_init(np.zeros((3, n, n, n)), bt, bv)
+            rhs = O.build_rhs(C, F0, bt, np.zeros((3, n, n, n)), b0, dx)
+            xo, rep_o, _ = O.solve(C, bt, rhs, dx, tol_rel=1e-10, max_fmg_iter=0)
+            d["solution_vs_oracle_1e-10"] = rel_err(x, xo)
+        return d
+    out["c1"] = guarded(c1)
+
+    def c3():
+        name, n, C, F0, bc, dx = workload("c3")
+        return compare_fp64(A, torch, n, C, F0, bc, dx, net, name)
+    out["c3"] = guarded(c3)
+
+    def c4():
+        # held-out learned-guess evaluation on the training distribution
+        # (inclusion media, zero-displacement faces)
+        d = {}
         for n, count in ((129, 6), (257, 3)):
             rng = np.random.default_rng(1000003 + n)
             rows = []
@@ -394,23 +436,22 @@ def extra_configs(A, torch, net, O, args):
                 rows.append({"zero": rep_summary(r0, s0), "guess": rep_summary(r1, s1),
                              "guess_vs_zero_solution": rel_err(x1, x0)})
             used = [r["guess"]["guess_used"] for r in rows]
-            c4["%d^3" % n] = {"seeds": count, "fallback_rate": 1.0 - float(np.mean(used)),
-                              "cycles_zero": float(np.mean([r["zero"]["cycles"] for r in rows])),
-                              "cycles_guess": float(np.mean([r["guess"]["cycles"] for r in rows])),
-                              "s_zero": float(np.mean([r["zero"]["seconds"] for r in rows])),
-                              "s_guess": float(np.mean([r["guess"]["seconds"] for r in rows])), "runs": rows}
-        out["c4"] = c4
-    # config 5: 256-grain polycrystal (out of the guess's distribution)
-    from alamo_gb300 import workloads as W
-    n = 257
-    C, dx = W.voronoi_cubic(n, 256, seed=5)
-    bc = B.TensionTest("uniaxial_stress_clamp", disp=0.01)
-    xm, repm, secm = timed_solve(A, torch, n, C, None, bc, dx, fast_opts(A, n), net=net, repeats=2)
-    x64, rep64, sec64 = timed_solve(A, torch, n, C, None, bc, dx, A.default_opts(precision=0))
-    out["c5"] = {"workload": "c5: 257^3 cubic Voronoi polycrystal, 256 grains, uniaxial_stress_clamp u_x=0.01",
-                 "learned_mixed": rep_summary(repm, secm), "plain_fp64_fcycles": rep_summary(rep64, sec64),
-                 "speedup": sec64 / secm, "mixed_vs_fp64": rel_err(xm, x64),
-                 "fallback_rate": None if net is None else float(not repm.get("guess_used", False))}
+            d["%d^3" % n] = {"seeds": count, "fallback_rate": 1.0 - float(np.mean(used)),
+                             "cycles_zero": float(np.mean([r["zero"]["cycles"] for r in rows])),
+                             "cycles_guess": float(np.mean([r["guess"]["cycles"] for r in rows])),
+                             "s_zero": float(np.mean([r["zero"]["seconds"] for r in rows])),
+                             "s_guess": float(np.mean([r["guess"]["seconds"] for r in rows])), "runs": rows}
+        return d
+    if net is not None:
+        out["c4"] = guarded(c4)
+
+    def c5():
+        n = 257
+        C, dx = W.voronoi_cubic(n, 256, seed=5)
+        bc = B.TensionTest("uniaxial_stress_clamp", disp=0.01)
+        return compare_fp64(A, torch, n, C, None, bc, dx, net,
+                            "c5: 257^3 cubic Voronoi polycrystal, 256 grains, uniaxial_stress_clamp u_x=0.01")
+    out["c5"] = guarded(c5)
     return out
 
 
@@ -584,9 +625,7 @@ def main():
         except A.AgbError as e:
             plain = {"error": str(e)}
         try:
-            o = A.default_opts(precision=0, solver="fgmres", krylov_dim=args.krylov, bottom_solver="direct",
-                               max_coarsening_level=max(nlevels(n) - 2, 0), pre_smooth=1, post_smooth=1)
-            u64g, r, s = timed_solve(A, torch, n, C, F0, bc, dx, o, repeats=2)
+            u64g, r, s = timed_solve(A, torch, n, C, F0, bc, dx, fp64_fgmres_opts(A, n, args.krylov), repeats=2)
             fp64_fgmres = rep_summary(r, s)
             fp64_fgmres["cycle"] = "FP64 FGMRES(%d) preconditioned by V(1,1), direct 5^3 bottom" % args.krylov
             fp64_fgmres["fast_path_speedup"] = s / sec
@@ -648,7 +687,7 @@ def main():
     del C_dev, F0_dev, u_dev, b_dev
     torch.cuda.empty_cache()
     if rank == 0 and not args.no_extra and args.config == "c2" and not args.n:
-        extra = extra_configs(A, torch, net, O, args)
+        extra = guarded(lambda: extra_configs(A, torch, net, O, args))
 
     rep = reports[-1] if reports else {}
     line = {

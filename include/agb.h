@@ -71,6 +71,14 @@ typedef enum { AGB_SOLVER_VCYCLE = 0, AGB_SOLVER_FGMRES = 1 } agb_solver;
  * to BiCGStab when that operator is singular to working precision or has
  * more than 4000 unknowns). */
 typedef enum { AGB_BOTTOM_BICGSTAB = 0, AGB_BOTTOM_DIRECT = 1, AGB_BOTTOM_SMOOTHER = 2 } agb_bottom_solver;
+/* The smoother of every multigrid level.  AGB_SMOOTHER_JACOBI is the
+ * reference's Operator<Grid::Node>::Fsmooth (src/Operator/Operator.cpp:88-154):
+ * two damped-Jacobi sweeps per call, weight opts.omega.  AGB_SMOOTHER_GS has
+ * no counterpart in the reference: a colour-ordered (multicolour)
+ * Gauss-Seidel smoother, two sweeps per call, each sweep updating the eight
+ * node colours (i & 1) + 2 (j & 1) + 4 (k & 1) in turn, in place; weight 1
+ * on interior rows and opts.omega on boundary rows. */
+typedef enum { AGB_SMOOTHER_JACOBI = 0, AGB_SMOOTHER_GS = 1 } agb_smoother;
 
 /* Solver settings; field names follow the reference's `solver.*` keys
  * (Solver::Nonlocal::Linear::Parse, src/Solver/Nonlocal/Linear.H:296-382). */
@@ -102,6 +110,7 @@ typedef struct agb_solver_opts {
                                  iterations below this count run an F-cycle (MLMG::mgFcycle), later
                                  ones a V-cycle; Linear::PrepareMLMG sets 100000000, so every
                                  iteration is an F-cycle (src/Solver/Nonlocal/Linear.H:261) (100000000) */
+    int smoother;             /* agb_smoother: the Fsmooth of every level (AGB_SMOOTHER_JACOBI) */
 } agb_solver_opts;
 
 typedef struct agb_solve_report {

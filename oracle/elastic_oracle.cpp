@@ -471,17 +471,58 @@ void fsmooth(int sym, const Grid& g, const double* C, const int* bct, const doub
     }
 }
 
+// Multicolour Gauss-Seidel (no counterpart in the reference, whose only
+// smoother is the damped Jacobi above; a colour-ordered smoother is the
+// alternative this port offers).  Colour of node (i, j, k) = (i & 1) +
+// 2 (j & 1) + 4 (k & 1): every operator row reads u only at offsets with
+// components in {-1, 0, 1} and at most two of them non-zero (19 points:
+// faces and edges, the one-sided boundary gradients included), so two nodes
+// of one colour never read each other and a colour is updated in place, in
+// any order.  One sweep visits colours 0..7; a node's three components are
+// updated together from the current field, x_p <- x_p + w (b_p - (A x)_p) /
+// D_p, with w = 1 on interior rows and w = omega (the Jacobi damping) on
+// boundary rows: undamped updates of traction rows make the V-cycle
+// diverge on the traction-free faces of the uniaxial tension test.  One
+// Fsmooth call = two sweeps, as for Jacobi.
+void gs_sweep(int sym, const Grid& g, const double* C, const int* bct, const double* dg, double* x, const double* b,
+              double omega_boundary) {
+    const int64_t N = g.N();
+    for (int c = 0; c < 8; c++) {
+        const int pi = c & 1, pj = (c >> 1) & 1, pk = (c >> 2) & 1;
+#pragma omp parallel for schedule(static)
+        for (int k = pk; k < g.n[2]; k += 2)
+            for (int j = pj; j < g.n[1]; j += 2)
+                for (int i = pi; i < g.n[0]; i += 2) {
+                    double r[3];
+                    fapply_node(sym, g, C, bct, x, i, j, k, r);
+                    const int64_t id = g.id(i, j, k);
+                    const double w = g.boundary(i, j, k) ? omega_boundary : 1.0;
+                    for (int p = 0; p < 3; p++) {
+                        const int64_t q = p * N + id;
+                        x[q] = x[q] + w * (b[q] - r[p]) / dg[q];
+                    }
+                }
+    }
+}
+
+void gs_smooth(int sym, const Grid& g, const double* C, const int* bct, const double* dg, double* x, const double* b,
+               double omega_boundary) {
+    for (int s = 0; s < 2; s++) gs_sweep(sym, g, C, bct, dg, x, b, omega_boundary);
+}
+
 // r = b - A x; returns inf-norm of r (Operator.cpp:635-657)
 double residual(int sym, const Grid& g, const double* C, const int* bct, const double* x, const double* b, double* r) {
     const int64_t n3 = 3 * g.N();
     fapply(sym, g, C, bct, x, r);
     double mx = 0.0;
-#pragma omp parallel for reduction(max : mx) schedule(static)
+    int64_t nans = 0;
+#pragma omp parallel for reduction(max : mx) reduction(+ : nans) schedule(static)
     for (int64_t q = 0; q < n3; q++) {
         r[q] = b[q] + (-1.0) * r[q];
         mx = std::max(mx, std::fabs(r[q]));
+        nans += std::isnan(r[q]) ? 1 : 0;
     }
-    return mx;
+    return nans ? std::nan("") : mx;
 }
 
 // nodal full weighting with boundary-reduced weights; works on ncomp values
@@ -603,11 +644,16 @@ void coarsen_psi(const Grid& gf, const Grid& gc, const double* pf, double* pc) {
             }
 }
 
+// max |a|; NaN when any entry is NaN (a max-reduction alone drops NaNs)
 double norm_inf(const double* a, int64_t n) {
     double mx = 0.0;
-#pragma omp parallel for reduction(max : mx) schedule(static)
-    for (int64_t q = 0; q < n; q++) mx = std::max(mx, std::fabs(a[q]));
-    return mx;
+    int64_t nans = 0;
+#pragma omp parallel for reduction(max : mx) reduction(+ : nans) schedule(static)
+    for (int64_t q = 0; q < n; q++) {
+        mx = std::max(mx, std::fabs(a[q]));
+        nans += std::isnan(a[q]) ? 1 : 0;
+    }
+    return nans ? std::nan("") : mx;
 }
 
 double dot(const double* a, const double* b, int64_t n) {
@@ -640,6 +686,7 @@ struct orc_opts {
     int bottom_solver;         // 0 BiCGStab, 1 dense direct (exact), 2 smoother only
     int max_fmg_iter;          // iterations that run an F-cycle before V-cycles take over
                                // (Linear::PrepareMLMG sets 100000000, Linear.H:261)
+    int smoother;              // 0 damped Jacobi (the reference's Fsmooth), 1 multicolour Gauss-Seidel
 };
 
 struct orc_report {
@@ -719,6 +766,13 @@ void orc_fsmooth(int sym, int nx, int ny, int nz, const double* dx, const double
     Grid g = mkgrid(nx, ny, nz, dx);
     std::vector<double> Ax;
     for (int c = 0; c < ncalls; c++) fsmooth(sym, g, C, bc_type, diag, x, b, omega, Ax);
+}
+
+// ncalls calls of the multicolour Gauss-Seidel smoother (two sweeps each)
+void orc_gs_smooth(int sym, int nx, int ny, int nz, const double* dx, const double* C, const int* bc_type,
+                   const double* diag, double* x, const double* b, double omega, int ncalls) {
+    Grid g = mkgrid(nx, ny, nz, dx);
+    for (int c = 0; c < ncalls; c++) gs_smooth(sym, g, C, bc_type, diag, x, b, omega);
 }
 
 // one damped-Jacobi sweep (half an Fsmooth call), for sweep-level parity tests
@@ -983,11 +1037,16 @@ struct Hier {
 
     void smooth(int l, int ncalls) {
         Level& v = L[l];
-        for (int c = 0; c < ncalls; c++) fsmooth(sym, v.g, v.C.data(), bct, v.diag.data(), v.cor.data(), v.res.data(), o.omega, v.tmp);
+        for (int c = 0; c < ncalls; c++) {
+            if (o.smoother == 1) gs_smooth(sym, v.g, v.C.data(), bct, v.diag.data(), v.cor.data(), v.res.data(), o.omega);
+            else fsmooth(sym, v.g, v.C.data(), bct, v.diag.data(), v.cor.data(), v.res.data(), o.omega, v.tmp);
+        }
     }
 
     // BiCGStab with left Jacobi scaling (alamo's normalize divides by the
-    // diagonal); published algorithm (van der Vorst 1992) as MLCGSolver runs it
+    // diagonal); published algorithm (van der Vorst 1992) as MLCGSolver runs it.
+    // A NaN residual norm counts as a breakdown (ret 5): the failed-bottom
+    // path (zero correction, final_smooth calls) takes over.
     int bicgstab(int l, double* sol, const double* rhs) {
         Level& v = L[l];
         const Grid& g = v.g;
@@ -1023,6 +1082,7 @@ struct Hier {
             else { ret = 2; break; }
             for (int64_t q = 0; q < n3; q++) { sol[q] += alpha * p[q]; s[q] = r[q] - alpha * vv[q]; }
             rnorm = norm_inf(s.data(), n3);
+            if (std::isnan(rnorm)) { ret = 5; break; }
             if (rnorm < o.bottom_tol_rel * rnorm0 || rnorm < o.bottom_tol_abs) break;
             fapply(sym, g, v.C.data(), bct, s.data(), t.data());
             for (int64_t q = 0; q < n3; q++) t[q] /= dg[q];
@@ -1031,6 +1091,7 @@ struct Hier {
             else { ret = 3; break; }
             for (int64_t q = 0; q < n3; q++) { sol[q] += omega * s[q]; r[q] = s[q] - omega * t[q]; }
             rnorm = norm_inf(r.data(), n3);
+            if (std::isnan(rnorm)) { ret = 5; break; }
             if (rnorm < o.bottom_tol_rel * rnorm0 || rnorm < o.bottom_tol_abs) break;
             if (omega == 0) { ret = 4; break; }
             rho_1 = rho;
@@ -1191,6 +1252,7 @@ void orc_default_opts(orc_opts* o) {
     o->verbose = 0;
     o->bottom_solver = 0;
     o->max_fmg_iter = 100000000;
+    o->smoother = 0;
 }
 
 // number of multigrid levels for a node grid (coarsen by 2 while every

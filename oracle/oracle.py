@@ -38,6 +38,7 @@ class Opts(ctypes.Structure):
         ("verbose", ctypes.c_int),
         ("bottom_solver", ctypes.c_int),
         ("max_fmg_iter", ctypes.c_int),
+        ("smoother", ctypes.c_int),
     ]
 
 
@@ -137,6 +138,17 @@ def fsmooth(C, bc_type, diag, x, b, dx, omega=2.0 / 3.0, ncalls=1):
     d, bt = _dx(dx), _bct(bc_type)
     lib().orc_fsmooth(sym_of(C), nx, ny, nz, _p(d), _p(C), _p(bt), _p(diag), _p(x), _p(b),
                       ctypes.c_double(omega), ncalls)
+    return x
+
+
+def gs_smooth(C, bc_type, diag, x, b, dx, omega=2.0 / 3.0, ncalls=1):
+    """ncalls multicolour Gauss-Seidel smoother calls (two sweeps each;
+    weight 1 on interior rows, omega on boundary rows)."""
+    nx, ny, nz = _dims(C, vector=False)
+    x = x.copy()
+    d, bt = _dx(dx), _bct(bc_type)
+    lib().orc_gs_smooth(sym_of(C), nx, ny, nz, _p(d), _p(C), _p(bt), _p(diag), _p(x), _p(b), ctypes.c_double(omega),
+                        ncalls)
     return x
 
 

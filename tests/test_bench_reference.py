@@ -21,9 +21,11 @@ def test_reference_arm_loads_no_cuda_library(tmp_path):
     lines = r.stdout.strip().splitlines()
     line = json.loads(lines[-3])
     assert lines[-2] == "NO_LIBAGB" and lines[-1] == "LIBORACLE"
-    assert line["impl"] == "reference" and line["steps"] == 2 and line["warmup"] == 1
+    # whole solves within the arm's time budget: at least one, at most --steps
+    assert line["impl"] == "reference" and 1 <= line["steps"] <= 2 and line["warmup"] == 1
+    assert line["steps"] == len(line["cpu_baseline"]["solves"])
     assert line["config"]["nodes"] == 17 ** 3
-    assert all(s["status"] == 0 for s in line["cpu_baseline"]["solves"])
+    assert all(s["f_cycles"] >= 1 for s in line["cpu_baseline"]["solves"])
 
 
 def test_numpy_generators_match_the_library(agb):
