@@ -15,10 +15,10 @@ EXPORTS = [
     "agb_elastic_set_stream", "agb_elastic_set_model", "agb_elastic_get_model", "agb_elastic_set_bc",
     "agb_elastic_prepare", "agb_elastic_num_levels", "agb_elastic_level_dims", "agb_elastic_fapply",
     "agb_elastic_fapply_f32", "agb_elastic_diagonal", "agb_elastic_fsmooth", "agb_elastic_residual",
-    "agb_elastic_fsmooth_f32", "agb_elastic_residual_f32",
+    "agb_elastic_fsmooth_f32", "agb_elastic_residual_f32", "agb_elastic_residual_dfloat",
     "agb_elastic_restrict", "agb_elastic_prolong_add", "agb_elastic_vcycle", "agb_elastic_bc_init", "agb_elastic_build_rhs",
     "agb_linear_solve", "agb_newton_solve", "agb_elastic_stress_strain", "agb_profile_enable",
-    "agb_profile_reset", "agb_profile_get", "agb_launch_count", "agb_cubic_stiffness", "agb_synth_uniform",
+    "agb_profile_reset", "agb_profile_get", "agb_profile_bytes", "agb_launch_count", "agb_cubic_stiffness", "agb_synth_uniform",
     "agb_synth_inclusion_iso", "agb_synth_voronoi_cubic", "agb_synth_spheres_iso", "agb_synth_spheres_diffuse",
     "agb_status_string",
     "agb_last_error", "agb_version", "agb_residual_norms_noalloc",
@@ -35,8 +35,9 @@ PRECISION_FP64, PRECISION_MIXED = 0, 1
 SOLVER_VCYCLE, SOLVER_FGMRES = 0, 1
 BOTTOM_BICGSTAB, BOTTOM_DIRECT, BOTTOM_SMOOTHER = 0, 1, 2
 SMOOTHER_JACOBI, SMOOTHER_GS = 0, 1
+OUTER_FP64, OUTER_DFLOAT = 0, 1
 K_FAPPLY_F64, K_JACOBI_F64, K_RESIDUAL_F64, K_FAPPLY_F32, K_JACOBI_F32, K_RESIDUAL_F32, K_RESTRICT, K_PROLONG, \
-    K_BOTTOM = range(9)
+    K_BOTTOM, K_KRYLOV, K_RESIDUAL_DF = range(11)
 
 
 class SolverOpts(ctypes.Structure):
@@ -65,6 +66,7 @@ class SolverOpts(ctypes.Structure):
         ("tma_min_nodes", ctypes.c_int),
         ("max_fmg_iter", ctypes.c_int),
         ("smoother", ctypes.c_int),
+        ("outer_residual", ctypes.c_int),
     ]
 
 

@@ -164,6 +164,25 @@ cudaError_t launch_dense_bottom(const double* Ainv, const double* rhs, double* s
 }  // namespace agb
 
 namespace agb {
+// Double-float outer residual of the mixed solve (residual_df.cu): hi + lo
+// FP32 pairs, 8 bytes per value (dfloat.cuh; only pointers cross into host
+// code).  r = b - A x written rounded to FP32 (r64 null) or in FP64 to r64,
+// per-block (max |r|, sum r^2) partials in the residual kernel's block
+// layout (residual_df_blocks).
+struct dfloat;
+constexpr int DFLOAT_BYTES = 8;
+cudaError_t launch_residual_df(int sym, const dfloat* x, const dfloat* b, const dfloat* C,
+                               const LevelGeom<double>& G, const BcTable& bc, float* r, double* r64,
+                               double* partials, int* nblocks_out, cudaStream_t s);
+int residual_df_blocks(int nx, int ny, int nz);
+cudaError_t launch_to_df(const double* src, dfloat* dst, int64_t n, cudaStream_t s);
+cudaError_t launch_df_to_double(const dfloat* src, double* dst, int64_t n, cudaStream_t s);
+// x += a e (e FP32)
+cudaError_t launch_df_axpy(const float* e, double a, dfloat* x, int64_t n, cudaStream_t s);
+cudaError_t launch_scale_f32(float* v, float a, int64_t n, cudaStream_t s);
+}  // namespace agb
+
+namespace agb {
 // message returned by agb_last_error() for the calling thread
 void set_last_error(const char* msg);
 }  // namespace agb

@@ -69,7 +69,7 @@ struct Lev {
     // FP32 levels swept by the TMA stencil kernels: stiffness with the x
     // pitch padded to 4 values and its tensor map
     T* Cpad = nullptr;
-    ZtMaps map{};
+    CUtensorMap map{};
     bool tma = false;
     // psi of this level (ghosted, LevelGeom::psi layout), owned; the FP64
     // fine level uses the handle's psi_fine instead
@@ -140,6 +140,12 @@ struct agb_elastic {
     bool psi_set = false;
     // NeoHookean model (mu, kappa) SoA of the finite-deformation Newton path
     double* nh_model = nullptr;
+    // double-float outer residual of the mixed solve (opts.outer_residual):
+    // the fine stiffness, solution and right-hand side as hi + lo FP32 pairs
+    dfloat* df_C = nullptr;
+    dfloat* df_x = nullptr;
+    dfloat* df_b = nullptr;
+    bool have_df = false;
     Krylov<double> K64;
     Krylov<float> K32;
     // dense direct bottom solve
@@ -156,6 +162,7 @@ struct agb_elastic {
     bool prof = false;
     int64_t prof_count[AGB_K_NFAMILIES] = {0};
     double prof_ms[AGB_K_NFAMILIES] = {0};
+    double prof_bytes[AGB_K_NFAMILIES] = {0};  // algorithmic bytes of the timed launches
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
     size_t ev_used = 0;
@@ -181,8 +188,9 @@ struct ProfScope {
     agb_elastic* h;
     int fam;
     cudaEvent_t a = nullptr, b = nullptr;
-    ProfScope(agb_elastic* hh, int f, bool on) : h(hh), fam(f) {
+    ProfScope(agb_elastic* hh, int f, bool on, double bytes = 0.0) : h(hh), fam(f) {
         if (!on || !h->prof) { h = nullptr; return; }
+        h->prof_bytes[f] += bytes;
         if (h->ev_used + 2 > h->ev_pool.size()) {
             for (int q = 0; q < 64; q++) {
                 cudaEvent_t e;
@@ -397,7 +405,7 @@ agb_status build_f32(agb_elastic* h) {
         CK(launch_recip(v.diag, v.dinv, 3 * G.N, h->stream));
         h->launches += 2;
         if (!v.tma) {
-            CK(make_stiffness_maps(v.Cpad, G.nx, G.ny, G.nz, h->nc, &v.map));
+            CK(make_stiffness_map(v.Cpad, G.nx, G.ny, G.nz, h->nc, &v.map));
             v.tma = true;
         }
     }
@@ -688,6 +696,44 @@ agb_status fcycle64(agb_elastic* h) {
 }
 
 // FP64 residual of level 0 into L64[0].res and its norms (host copy)
+// double-float state of the mixed solve: the fine stiffness as hi + lo
+// pairs (rebuilt when the model changes) and room for the solution and the
+// right-hand side
+agb_status ensure_df(agb_elastic* h) {
+    const Lev<double>& top = h->L64[0];
+    const int64_t N = top.G.N;
+    if (!h->df_C) CK(cudaMalloc(&h->df_C, (size_t)DFLOAT_BYTES * N * h->nc));
+    if (!h->df_x) CK(cudaMalloc(&h->df_x, (size_t)DFLOAT_BYTES * 3 * N));
+    if (!h->df_b) CK(cudaMalloc(&h->df_b, (size_t)DFLOAT_BYTES * 3 * N));
+    if (!h->have_df) {
+        CK(launch_to_df(top.C, h->df_C, N * h->nc, h->stream));
+        h->launches++;
+        h->have_df = true;
+    }
+    return AGB_OK;
+}
+
+// double-float residual of df_x against df_b into the fine FP32 level's
+// rescor (unscaled, rounded to FP32) and its norms (host copy)
+agb_status residual_df(agb_elastic* h, double out[2]) {
+    const Lev<double>& top = h->L64[0];
+    int nb = 0;
+    {
+        // x, b (3 pairs each), the stiffness pairs in; r (3 floats) out
+        const double bytes = (double)top.G.N * (DFLOAT_BYTES * (6 + h->nc) + 12);
+        ProfScope ps(h, AGB_K_RESIDUAL_DF, true, bytes);
+        CK(launch_residual_df(h->sym, h->df_x, h->df_b, h->df_C, top.G, h->bc, h->L32[0].rescor, nullptr,
+                              h->partials, &nb, h->stream));
+    }
+    CK(launch_reduce_norms(h->partials, nb, h->norms_dev, h->stream));
+    h->launches += 2;
+    CK(cudaMemcpyAsync(h->norms_host, h->norms_dev, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    out[0] = h->norms_host[0];
+    out[1] = h->norms_host[1];
+    return AGB_OK;
+}
+
 agb_status residual64(agb_elastic* h, const double* x, const double* rhs, double out[2]) {
     Lev<double>& v = h->L64[0];
     int nb = 0;
@@ -762,8 +808,12 @@ agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, doub
     Krylov<T>& K = krylov_of<T>(h);
     cudaStream_t st = h->stream;
     // beta = ||r||_2
+    const double vb = (double)sizeof(T) * n;  // bytes of one Krylov vector
     CK(cudaMemcpyAsync(K.w, r, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
-    CK(launch_multidot<T>(K.Wdev, 1, K.w, n, K.part, K.dots, st));
+    {
+        ProfScope ps(h, AGB_K_KRYLOV, true, vb);
+        CK(launch_multidot<T>(K.Wdev, 1, K.w, n, K.part, K.dots, st));
+    }
     CK(cudaMemcpyAsync(K.hdots, K.dots, sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     h->launches += 2;
@@ -774,7 +824,10 @@ agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, doub
         CK(cudaMemsetAsync(K.e, 0, sizeof(T) * n, st));
         return AGB_OK;
     }
-    CK(launch_scale_copy<T>(r, K.V[0], n, 1.0 / beta, st));
+    {
+        ProfScope ps(h, AGB_K_KRYLOV, true, 2 * vb);
+        CK(launch_scale_copy<T>(r, K.V[0], n, 1.0 / beta, st));
+    }
     h->launches++;
     std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m, 0.0), sn(m, 0.0), g(m + 1, 0.0);
     g[0] = beta;
@@ -807,13 +860,20 @@ agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, doub
         // classical Gram-Schmidt, re-orthogonalised once unless krylov_reorth = 0
         // (the last projection also leaves ||w||^2 in dots[80])
         const bool reorth = h->opts.krylov_reorth != 0;
-        CK(launch_multidot<T>(K.Vdev, j + 1, K.w, n, K.part, K.dots, st));
-        if (reorth) {
-            CK(launch_multiaxpy<T>(K.w, 1.0, K.Vdev, K.dots, -1.0, j + 1, n, st));
-            CK(launch_multidot<T>(K.Vdev, j + 1, K.w, n, K.part, K.dots + 40, st));
-            CK(launch_multiaxpy_norm<T>(K.w, 1.0, K.Vdev, K.dots + 40, -1.0, j + 1, n, K.part, K.dots + 80, st));
-        } else {
-            CK(launch_multiaxpy_norm<T>(K.w, 1.0, K.Vdev, K.dots, -1.0, j + 1, n, K.part, K.dots + 80, st));
+        {
+            // algorithmic bytes: each pass of dots reads V_0..V_j and w; each
+            // projection reads them and writes w
+            const double gs_bytes = (reorth ? 2 : 1) * ((j + 2) + (j + 3)) * vb;
+            ProfScope ps(h, AGB_K_KRYLOV, true, gs_bytes);
+            CK(launch_multidot<T>(K.Vdev, j + 1, K.w, n, K.part, K.dots, st));
+            if (reorth) {
+                CK(launch_multiaxpy<T>(K.w, 1.0, K.Vdev, K.dots, -1.0, j + 1, n, st));
+                CK(launch_multidot<T>(K.Vdev, j + 1, K.w, n, K.part, K.dots + 40, st));
+                CK(launch_multiaxpy_norm<T>(K.w, 1.0, K.Vdev, K.dots + 40, -1.0, j + 1, n, K.part, K.dots + 80,
+                                            st));
+            } else {
+                CK(launch_multiaxpy_norm<T>(K.w, 1.0, K.Vdev, K.dots, -1.0, j + 1, n, K.part, K.dots + 80, st));
+            }
         }
         CK(cudaMemcpyAsync(K.hdots, K.dots, sizeof(double) * 120, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -822,6 +882,7 @@ agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, doub
         const double hn = std::sqrt(std::max(K.hdots[80], 0.0));
         H[(size_t)(j + 1) * m + j] = hn;
         if (hn > 0.0) {
+            ProfScope ps(h, AGB_K_KRYLOV, true, 2 * vb);
             CK(launch_scale_copy<T>(K.w, K.V[j + 1], n, 1.0 / hn, st));
             h->launches++;
         }
@@ -852,7 +913,10 @@ agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, doub
     }
     std::memcpy(K.hdots, y.data(), sizeof(double) * k);
     CK(cudaMemcpyAsync(K.dots, K.hdots, sizeof(double) * k, cudaMemcpyHostToDevice, st));
-    CK(launch_multiaxpy<T>(K.e, 0.0, K.Zdev, K.dots, 1.0, k, n, st));
+    {
+        ProfScope ps(h, AGB_K_KRYLOV, true, (k + 1) * vb);
+        CK(launch_multiaxpy<T>(K.e, 0.0, K.Zdev, K.dots, 1.0, k, n, st));
+    }
     h->launches++;
     *its = k;
     *est = resid / beta;
@@ -887,10 +951,34 @@ agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_re
     }
     int fp64_res = 0;
     bool r_exact = true;  // r is an FP64 residual (or rhs itself)
+    // double-float outer residual and update (mixed FGMRES without psi): the
+    // iterate lives in df_x during the solve and x receives it at the end;
+    // r_f32: the current residual is in the fine FP32 level's rescor
+    // (unscaled) instead of the FP64 level's res
+    const bool use_df = mixed && h->opts.solver == AGB_SOLVER_FGMRES &&
+                        h->opts.outer_residual == AGB_OUTER_DFLOAT && !h->psi_set;
+    bool r_f32 = false;
+    if (use_df) {
+        TRY(ensure_df(h));
+        CK(launch_to_df(rhs, h->df_b, n3, h->stream));
+        if (x_zero) CK(cudaMemsetAsync(h->df_x, 0, (size_t)DFLOAT_BYTES * n3, h->stream));
+        else CK(launch_to_df(x, h->df_x, n3, h->stream));
+        h->launches += 2;
+    }
     if (x_zero) {
-        CK(cudaMemcpyAsync(top.res, rhs, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+        if (use_df) {
+            CK(launch_from_double<float>(rhs, h->L32[0].rescor, n3, 1.0, h->stream));
+            h->launches++;
+            r_f32 = true;
+        } else {
+            CK(cudaMemcpyAsync(top.res, rhs, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+        }
         r[0] = bn[0];
         r[1] = bn[1];
+    } else if (use_df && !r32_init) {
+        TRY(residual_df(h, r));
+        fp64_res = 1;
+        r_f32 = true;
     } else if (mixed && r32_init) {
         CK(cudaMemsetAsync(top.res, 0, sizeof(double) * n3, h->stream));
         CK(launch_add_float(r32_init, top.res, n3, 1.0, h->stream));
@@ -923,10 +1011,12 @@ agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_re
                     const double need = 0.1 * target / std::max(r[0], 1e-300);
                     const double rel = std::min(std::max(h->opts.inner_tol, need), 0.5);
                     Lev<float>& t32 = h->L32[0];
-                    CK(launch_from_double<float>(top.res, t32.rescor, n3, s, h->stream));
+                    if (r_f32) CK(launch_scale_f32(t32.rescor, (float)s, n3, h->stream));
+                    else CK(launch_from_double<float>(top.res, t32.rescor, n3, s, h->stream));
                     h->launches++;
                     TRY(fgmres_cycle<float>(h, h->L32, t32.rescor, rel, maxit - it, &its, &est));
-                    CK(launch_axpy_to_double<float>(h->K32.e, x, n3, 1.0 / s, h->stream));
+                    if (use_df) CK(launch_df_axpy(h->K32.e, 1.0 / s, h->df_x, n3, h->stream));
+                    else CK(launch_axpy_to_double<float>(h->K32.e, x, n3, 1.0 / s, h->stream));
                 } else {
                     // FP64 FGMRES(V-cycle); aim a little below the target, the true residual decides
                     const double rt = std::max(0.5 * target / std::max(r[0], 1e-300), 1e-15);
@@ -963,13 +1053,22 @@ agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_re
                     }
                 }
             }
-            TRY(residual64(h, x, rhs, r));
+            if (use_df) {
+                TRY(residual_df(h, r));
+                r_f32 = true;
+            } else {
+                TRY(residual64(h, x, rhs, r));
+            }
             fp64_res++;
             if (h->opts.verbose > 0) std::fprintf(stderr, "agb: cycle %d |r|_inf = %.6e\n", it, r[0]);
             if (std::isnan(r[0]) || std::isnan(r[1])) { status = AGB_NAN; break; }
             if (r[0] <= target && !fixed) { status = AGB_OK; break; }
         }
         if (fixed && status != AGB_NAN) status = AGB_OK;
+    }
+    if (use_df) {
+        CK(launch_df_to_double(h->df_x, x, n3, h->stream));
+        h->launches++;
     }
     int binfo[4] = {0, 0, 0, 0};
     CK(cudaMemcpyAsync(h->norms_host, h->bottom_info, 4 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -1063,6 +1162,7 @@ agb_status agb_default_opts(agb_solver_opts* o) {
     o->tma_min_nodes = 0;
     o->max_fmg_iter = 100000000;
     o->smoother = AGB_SMOOTHER_JACOBI;
+    o->outer_residual = AGB_OUTER_FP64;
     return AGB_OK;
 }
 
@@ -1080,6 +1180,8 @@ static agb_status check_opts(const agb_solver_opts* o) {
     if (o->tma_min_nodes < 0) return fail(AGB_BAD_ARG, "tma_min_nodes must be >= 0");
     if (o->smoother != AGB_SMOOTHER_JACOBI && o->smoother != AGB_SMOOTHER_GS)
         return fail(AGB_BAD_ARG, "unknown smoother");
+    if (o->outer_residual != AGB_OUTER_FP64 && o->outer_residual != AGB_OUTER_DFLOAT)
+        return fail(AGB_BAD_ARG, "unknown outer_residual");
     if (o->solver == AGB_SOLVER_FGMRES && (o->krylov_dim < 1 || o->krylov_dim > 39))
         return fail(AGB_BAD_ARG, "krylov_dim must lie in [1, 39]");
     if (o->solver == AGB_SOLVER_FGMRES && !(o->inner_tol > 0.0 && o->inner_tol < 1.0))
@@ -1140,6 +1242,9 @@ agb_status agb_elastic_destroy(agb_elastic* h) {
     cudaFree(h->dw);
     cudaFree(h->psi_fine);
     cudaFree(h->nh_model);
+    cudaFree(h->df_C);
+    cudaFree(h->df_x);
+    cudaFree(h->df_b);
     h->K64.release();
     h->K32.release();
     cudaFree(h->bot_inv);
@@ -1168,6 +1273,7 @@ agb_status agb_elastic_set_opts(agb_elastic* h, const agb_solver_opts* o) {
         }
         free_levels(h->L32);
         h->have_f32 = false;
+        h->have_df = false;
         agb_status st = alloc_levels64(h);
         if (st == AGB_OK && keep)
             st = (cudaMemcpy(h->L64[0].C, keep, sizeof(double) * N * h->nc, cudaMemcpyDeviceToDevice) == cudaSuccess)
@@ -1178,6 +1284,7 @@ agb_status agb_elastic_set_opts(agb_elastic* h, const agb_solver_opts* o) {
     }
     h->prepared = false;
     h->have_f32 = false;
+    h->have_df = false;
     h->bot_src = 0;
     return AGB_OK;
 }
@@ -1212,6 +1319,7 @@ agb_status agb_elastic_set_model(agb_elastic* h, const double* C, int where) {
     h->model_set = true;
     h->prepared = false;
     h->have_f32 = false;
+    h->have_df = false;
     h->bot_src = 0;
     return AGB_OK;
 }
@@ -1237,6 +1345,7 @@ agb_status agb_elastic_set_bc(agb_elastic* h, const int* type, const double* val
     h->bc_set = true;
     h->prepared = false;
     h->have_f32 = false;
+    h->have_df = false;
     h->bot_src = 0;
     return AGB_OK;
 }
@@ -1277,6 +1386,7 @@ agb_status agb_elastic_set_psi(agb_elastic* h, const double* psi, double small, 
     }
     h->prepared = false;
     h->have_f32 = false;
+    h->have_df = false;
     h->bot_src = 0;
     return AGB_OK;
 }
@@ -1438,6 +1548,39 @@ agb_status agb_elastic_residual_f32(agb_elastic* h, int level, const float* x, c
     }
     h->launches++;
     TRY(finish_out(h, r, dr, bytes, where));
+    prof_collect(h);
+    return AGB_OK;
+}
+
+agb_status agb_elastic_residual_dfloat(agb_elastic* h, const double* x, const double* b, double* r, double norms[2],
+                                       int where) {
+    TRY(check_level(h, 0));
+    if (!x || !b || !r) return fail(AGB_BAD_ARG, "null argument");
+    if (h->psi_set) return fail(AGB_BAD_ARG, "the double-float residual has no psi terms");
+    if (!h->model_set) return fail(AGB_NOT_READY, "model not set (agb_elastic_set_model)");
+    TRY(ensure_df(h));
+    Lev<double>& v = h->L64[0];
+    const int64_t n3 = 3 * v.G.N;
+    const size_t bytes = sizeof(double) * n3;
+    const void* dx0 = nullptr;
+    const void* db = nullptr;
+    void* dr = nullptr;
+    TRY(dev_in(h, 0, x, bytes, where, &dx0));
+    TRY(dev_in(h, 1, b, bytes, where, &db));
+    TRY(dev_out(h, 2, r, bytes, where, &dr));
+    CK(launch_to_df((const double*)dx0, h->df_x, n3, h->stream));
+    CK(launch_to_df((const double*)db, h->df_b, n3, h->stream));
+    int nb = 0;
+    {
+        ProfScope ps(h, AGB_K_RESIDUAL_DF, true, (double)v.G.N * (DFLOAT_BYTES * (6 + h->nc) + 24));
+        CK(launch_residual_df(h->sym, h->df_x, h->df_b, h->df_C, v.G, h->bc, nullptr, (double*)dr, h->partials, &nb,
+                              h->stream));
+    }
+    CK(launch_reduce_norms(h->partials, nb, h->norms_dev, h->stream));
+    h->launches += 4;
+    CK(cudaMemcpyAsync(h->norms_host, h->norms_dev, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TRY(finish_out(h, r, dr, bytes, where));
+    if (norms) { norms[0] = h->norms_host[0]; norms[1] = h->norms_host[1]; }
     prof_collect(h);
     return AGB_OK;
 }
@@ -1796,6 +1939,7 @@ agb_status agb_newton_solve_neohookean(agb_elastic* h, const double* model, doub
         h->model_set = true;
         h->prepared = false;
         h->have_f32 = false;
+        h->have_df = false;
         h->bot_src = 0;
         CK(launch_rhs_from_dw((const double*)du, (const double*)db, h->dw, h->L64[0].G, h->bc, rhs, h->stream));
         h->launches += 2;
@@ -1840,7 +1984,13 @@ agb_status agb_profile_enable(agb_elastic* h, int on) {
 agb_status agb_profile_reset(agb_elastic* h) {
     if (!h) return fail(AGB_BAD_ARG, "null handle");
     prof_collect(h);
-    for (int f = 0; f < AGB_K_NFAMILIES; f++) { h->prof_count[f] = 0; h->prof_ms[f] = 0.0; }
+    for (int f = 0; f < AGB_K_NFAMILIES; f++) { h->prof_count[f] = 0; h->prof_ms[f] = 0.0; h->prof_bytes[f] = 0.0; }
+    return AGB_OK;
+}
+
+agb_status agb_profile_bytes(agb_elastic* h, int family, double* bytes) {
+    if (!h || !bytes || family < 0 || family >= AGB_K_NFAMILIES) return fail(AGB_BAD_ARG, "bad argument");
+    *bytes = h->prof_bytes[family];
     return AGB_OK;
 }
 

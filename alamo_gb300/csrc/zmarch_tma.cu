@@ -5,20 +5,14 @@
 // x and y, so the 255 interior columns of a 257-node axis fill 8 tiles of 32
 // exactly) through a chunk of z-planes.  Per plane it needs
 //   * the displacement of planes k-1, k, k+1 with a one-node x/y halo
-//     (10 x 34 nodes): a ring filled by 4-byte cp.async, plane k+1+DIST
-//     issued at the top of step k, the three components of a node
-//     interleaved in one 16-byte cell so a stencil point is one 128-bit
-//     shared load;
+//     (3 x 10 x 34 values): a 4-slot ring filled by 4-byte cp.async, plane
+//     k+2 issued at the top of step k;
 //   * the stiffness of plane k with the x/y halo (for the in-plane
 //     derivatives of C) and of plane k+1 at the block's own columns (for
-//     the z-derivative): a ring of TMA boxes (36 x 10 nodes), plane
-//     k+1+DIST issued at the top of step k into the slot plane k-1 has
-//     left; the stiffness of plane k-1 at the own column is kept in
-//     registers from the previous step.  The major-minor copy is stored
-//     as five float4 groups (entries 4g..4g+3, one 16-byte cell per node)
-//     plus entry 20 on its own, so a node's 21 entries are five 128-bit
-//     shared loads and one 32-bit load; the groups arrive by one 5-D box
-//     (4 x 36 x 10 x 1 x 5), entry 20 by a 4-D one, on the same mbarrier.
+//     the z-derivative): a 3-slot ring of TMA boxes (36 x 10 nodes x NC
+//     entries), plane k+2 issued at the top of step k into the slot plane
+//     k-1 has left; the stiffness of plane k-1 at the own column is kept in
+//     registers from the previous step.
 // Everything the stencil reads then comes from shared memory at offsets that
 // are compile-time constants, and each array is read from HBM about once per
 // sweep.  The six boundary faces (2.3% of the nodes at 257^3) run in a
@@ -26,7 +20,7 @@
 // every step of the edge tiles back at the block barrier.  The TMA box
 // starts at x = x0 - 1 = 32 * blockIdx.x, a multiple of 4 floats (16 bytes);
 // the stiffness copy it reads has its x pitch padded to a multiple of 4
-// nodes so every global stride is a multiple of 16 bytes.
+// floats so every global stride is a multiple of 16 bytes.
 //
 // Every wait on an mbarrier is bounded: after the limit the block records
 // the failure in *err, stops marching (uniformly, through a shared flag),
@@ -50,13 +44,10 @@ namespace {
 
 constexpr int TX = 32, TY = 8, NT = TX * TY;
 constexpr int UHX = TX + 2, UHY = TY + 2;
-constexpr int UVAL = 3 * UHY * UHX;               // displacement values per staged plane
-constexpr int UPL = 4 * UHY * UHX;                // floats per staged plane (3 + 1 pad per node)
-constexpr int U_PER_T = (UVAL + NT - 1) / NT;     // cp.async per thread per plane
+constexpr int UPL = 3 * UHY * UHX;                // displacement values per staged plane
+constexpr int U_PER_T = (UPL + NT - 1) / NT;      // cp.async per thread per plane
 constexpr int CBX = 36, CBY = 10;                 // TMA box (x, y) of a stiffness plane
-constexpr int CEL = CBX * CBY;                    // nodes of a stiffness box
-constexpr int NG = 5;                             // float4 groups of the major-minor copy (entries 0..19)
-constexpr int GEL = 4 * CEL;                      // floats per float4 group in a slot
+constexpr int CEL = CBX * CBY;                    // floats per stiffness entry in a slot
 constexpr uint64_t WAIT_NS = 1000000000ull;       // 1 s: a TMA load takes microseconds
 
 // Prefetch distance and ring sizes.  Step k reads planes k-1 (displacement;
@@ -120,18 +111,6 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map
         "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(e), "r"(bar)
         : "memory");
 }
-__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map, int c0, int x, int y, int z, int g,
-                                            uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(x), "r"(y), "r"(z), "r"(g), "r"(bar)
-        : "memory");
-}
-__device__ __forceinline__ float4 lds4(const float* p) { return *reinterpret_cast<const float4*>(p); }
-__device__ __forceinline__ float comp(const float4& v, int c) {
-    return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
-}
 __device__ __forceinline__ void cp_async4(uint32_t dst, const float* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
 }
@@ -145,12 +124,10 @@ __device__ __forceinline__ void cp_async_wait_group() {
 
 template <int SYM, int MODE>
 __global__ void __launch_bounds__(NT, 2)
-    k_zmarch_tma(const __grid_constant__ CUtensorMap cmap, const __grid_constant__ CUtensorMap cmap2,
-                 const float* __restrict__ x, LevelGeom<float> G, const float* __restrict__ b,
-                 const float* __restrict__ dg, float omega, float* __restrict__ out, int kchunk,
-                 int* __restrict__ err) {
+    k_zmarch_tma(const __grid_constant__ CUtensorMap cmap, const float* __restrict__ x, LevelGeom<float> G,
+                 const float* __restrict__ b, const float* __restrict__ dg, float omega, float* __restrict__ out,
+                 int kchunk, int* __restrict__ err) {
     constexpr int NC = SYM == SYM_ISO ? 2 : 21;
-    constexpr bool VQ = SYM == SYM_MM;  // float4-grouped stiffness
     using SM = ZtSmem<NC>;
     constexpr int CS = SM::CS, US = SM::US, DIST = SM::DIST;
     extern __shared__ unsigned char zt_raw[];
@@ -181,8 +158,8 @@ __global__ void __launch_bounds__(NT, 2)
         const int q = tid + r * NT;
         const int p = q / (UHY * UHX), rem = q - p * (UHY * UHX), yy = rem / UHX, xx = rem - yy * UHX;
         const int gx = x0 - 1 + xx, gy = y0 - 1 + yy;
-        soff[r] = 4 * rem + p;  // components of a node interleaved
-        gval[r] = (q < UVAL) & (gx < G.nx) & (gy < G.ny);
+        soff[r] = q;
+        gval[r] = (q < UPL) & (gx < G.nx) & (gy < G.ny);
         goff[r] = p * N + gx + sy * gy;
     }
     // one commit group per call (planes past the chunk commit an empty
@@ -202,28 +179,13 @@ __global__ void __launch_bounds__(NT, 2)
     auto issue_u = [&](int kk, bool real) { issue_u_at(kk, kk % US, real); };
     auto issue_c_at = [&](int kk, int s) {  // one thread
         mbar_expect_tx(bar_u32 + 8u * s, SM::box_bytes);
-        const uint32_t dst = cs_u32 + (uint32_t)(s * SM::slot_bytes);
-        if (VQ) {
-            tma_load_5d(dst, &cmap, 0, TX * blockIdx.x, TY * blockIdx.y, kk, 0, bar_u32 + 8u * s);
-            tma_load_4d(dst + NG * GEL * 4, &cmap2, TX * blockIdx.x, TY * blockIdx.y, kk, 0, bar_u32 + 8u * s);
-        } else {
-            tma_load_4d(dst, &cmap, TX * blockIdx.x, TY * blockIdx.y, kk, 0, bar_u32 + 8u * s);
-        }
+        tma_load_4d(cs_u32 + (uint32_t)(s * SM::slot_bytes), &cmap, TX * blockIdx.x, TY * blockIdx.y, kk, 0,
+                    bar_u32 + 8u * s);
     };
     auto issue_c = [&](int kk) { issue_c_at(kk, kk % CS); };
     // plane kk is the n-th load into its slot, n = (kk - (k0 - 1)) / CS
     auto parity = [&](int kk) { return (uint32_t)(((kk - (k0 - 1)) / CS) & 1); };
-    // entry e of the stiffness at node offset (a, bb) from this thread's
-    // node in a slot (VQ: group e/4 component e%4, entry 20 after the groups)
-    const int oc = (ty + 1) * CBX + (tx + 1);
-    auto centry = [&](const float* slot, int e, int a, int bb) -> float {
-        if (VQ) {
-            if (e < 4 * NG) return comp(lds4(slot + (e >> 2) * GEL + 4 * (oc + bb * CBX + a)), e & 3);
-            return slot[NG * GEL + oc + bb * CBX + a];
-        }
-        return slot[e * CEL + oc + bb * CBX + a];
-    };
-    auto cslot = [&](int kk) { return Cs + (kk % CS) * (SM::slot_bytes / 4); };
+    auto cslot = [&](int kk) { return Cs + (kk % CS) * (SM::slot_bytes / 4) + (ty + 1) * CBX + (tx + 1); };
 
     if (tid == 0) {
         abort_flag = 0;
@@ -270,7 +232,7 @@ __global__ void __launch_bounds__(NT, 2)
     {
         const float* c = cslot(k0 - 1);
 #pragma unroll
-        for (int e = 0; e < NC; e++) Cp[e] = centry(c, e, 0, 0);
+        for (int e = 0; e < NC; e++) Cp[e] = c[e * CEL];
     }
     // the first step reloads the slot of plane k0 - 1: everyone has read it
     __syncthreads();
@@ -301,7 +263,8 @@ __global__ void __launch_bounds__(NT, 2)
     int sw = (k0 + 2) % CS;
     uint32_t pw = parity(k0 + 2);
     const int sbase = (k0 - 1) % CS;  // a slot's load count grows when the plane index passes it
-    const int o = 4 * ((ty + 1) * UHX + (tx + 1));
+    const int o = (ty + 1) * UHX + (tx + 1);
+    const int oc = (ty + 1) * CBX + (tx + 1);
     for (int k = k0; k < k1 && !abort_flag; k++) {
         if (!RC) {
             su = k % US;
@@ -324,26 +287,26 @@ __global__ void __launch_bounds__(NT, 2)
         const int64_t id = i + sy * j + sz * (int64_t)k;
         float bn[3] = {0.f, 0.f, 0.f}, dn[3] = {1.f, 1.f, 1.f};
         load_bd(k + 1, bn, dn);
-        const float* cc = Cs + sc * (SM::slot_bytes / 4);
+        const float* cc = Cs + sc * (SM::slot_bytes / 4) + oc;
         if (col) {
-            const float* cn = Cs + wrap(sc + 1, CS) * (SM::slot_bytes / 4);
+            const float* cn = Cs + wrap(sc + 1, CS) * (SM::slot_bytes / 4) + oc;
             const float* u0 = Us + su * UPL + o;
             const float* um = Us + wrap(su + US - 1, US) * UPL + o;
             const float* up = Us + wrap(su + 1, US) * UPL + o;
             auto U = [&](int p, int a, int bb, int c) -> float {
                 const float* s = c == 0 ? u0 : (c < 0 ? um : up);
-                return comp(lds4(s + 4 * (bb * UHX + a)), p);
+                return s[p * (UHY * UHX) + bb * UHX + a];
             };
             // the own column's stiffness of plane k, read once: the stencil's
             // centre entries and, for the next step, the plane-below values
             float c0[NC];
 #pragma unroll
-            for (int e = 0; e < NC; e++) c0[e] = centry(cc, e, 0, 0);
+            for (int e = 0; e < NC; e++) c0[e] = cc[e * CEL];
             auto Cf = [&](int e, int a, int bb, int c) -> float {
-                if (c > 0) return centry(cn, e, 0, 0);
+                if (c > 0) return cn[e * CEL];
                 if (c < 0) return Cp[e];
                 if (a == 0 && bb == 0) return c0[e];
-                return centry(cc, e, a, bb);
+                return cc[e * CEL + bb * CBX + a];
             };
             float r[3];
             interior_rows<float, SYM>(U, Cf, G, r);
@@ -353,7 +316,7 @@ __global__ void __launch_bounds__(NT, 2)
                 if (MODE == 0) {
                     out[q] = r[c];
                 } else if (MODE == 1) {
-                    const float xv = u0[c];
+                    const float xv = u0[c * (UHY * UHX)];
                     out[q] = xv + omega * (bq[c] - r[c]) * dq[c];
                 } else {
                     out[q] = bq[c] - r[c];
@@ -453,31 +416,6 @@ __global__ void k_pad_planes(const float* __restrict__ src, float* __restrict__ 
     }
 }
 
-// FP32 major-minor stiffness, SoA (21, nz, ny, nx) -> five float4 groups
-// (5, nz, ny, px, 4) followed by entry 20 (nz, ny, px); zero pad
-__global__ void k_pack_mm(const float* __restrict__ src, float* __restrict__ dst, int nx, int px, int64_t rows) {
-    const int64_t plane = rows * px;  // nodes of the padded copy
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < plane;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t row = t / px;
-        const int xx = (int)(t - row * px);
-        const bool in = xx < nx;
-        const int64_t sidx = row * nx + xx, N = rows * nx;
-#pragma unroll
-        for (int g = 0; g < NG; g++) {
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (in) {
-                v.x = src[(4 * g + 0) * N + sidx];
-                v.y = src[(4 * g + 1) * N + sidx];
-                v.z = src[(4 * g + 2) * N + sidx];
-                v.w = src[(4 * g + 3) * N + sidx];
-            }
-            reinterpret_cast<float4*>(dst)[g * plane + t] = v;
-        }
-        dst[4 * NG * plane + t] = in ? src[20 * N + sidx] : 0.f;
-    }
-}
-
 // planes per block: enough blocks for about two waves of two blocks per SM,
 // at least 4 planes (each block stages 3 extra planes), at most 32
 int zt_kchunk(int ni, int nj, int nk) {
@@ -497,8 +435,7 @@ bool zmarch_tma_supported(int nx, int ny, int nz) {
 
 int64_t zmarch_tma_pitch(int nx) { return (nx + 3) / 4 * 4; }
 
-static cudaError_t encode_tiled(CUtensorMap* map, int rank, const float* base, const cuuint64_t* dims,
-                                const cuuint64_t* strides, const cuuint32_t* box) {
+cudaError_t make_stiffness_map(const float* Cpad, int nx, int ny, int nz, int nc, CUtensorMap* map) {
     using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -511,46 +448,19 @@ static cudaError_t encode_tiled(CUtensorMap* map, int rank, const float* base, c
         if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorSymbolNotFound;
         encode = reinterpret_cast<EncodeFn>(fn);
     }
-    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
-    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank, const_cast<float*>(base), dims,
-                              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+    const int64_t px = zmarch_tma_pitch(nx);
+    const cuuint64_t dims[4] = {(cuuint64_t)px, (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)nc};
+    const cuuint64_t strides[3] = {(cuuint64_t)px * 4, (cuuint64_t)px * ny * 4, (cuuint64_t)px * ny * nz * 4};
+    const cuuint32_t box[4] = {(cuuint32_t)CBX, (cuuint32_t)CBY, 1u, (cuuint32_t)nc};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(Cpad), dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-cudaError_t make_stiffness_maps(const float* Cpad, int nx, int ny, int nz, int nc, ZtMaps* maps) {
-    const int64_t px = zmarch_tma_pitch(nx);
-    const cuuint64_t plane = (cuuint64_t)px * ny * nz;  // nodes of the padded copy
-    if (nc == 21) {
-        // five float4 groups: (4, x, y, z, group), box 4 x 36 x 10 x 1 x 5
-        const cuuint64_t dims[5] = {4, (cuuint64_t)px, (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)NG};
-        const cuuint64_t strides[4] = {16, (cuuint64_t)px * 16, (cuuint64_t)px * ny * 16, plane * 16};
-        const cuuint32_t box[5] = {4, (cuuint32_t)CBX, (cuuint32_t)CBY, 1u, (cuuint32_t)NG};
-        cudaError_t e = encode_tiled(&maps->main, 5, Cpad, dims, strides, box);
-        if (e != cudaSuccess) return e;
-        // entry 20: (x, y, z, 1), box 36 x 10 x 1 x 1
-        const cuuint64_t d2[4] = {(cuuint64_t)px, (cuuint64_t)ny, (cuuint64_t)nz, 1};
-        const cuuint64_t s2[3] = {(cuuint64_t)px * 4, (cuuint64_t)px * ny * 4, plane * 4};
-        const cuuint32_t b2[4] = {(cuuint32_t)CBX, (cuuint32_t)CBY, 1u, 1u};
-        return encode_tiled(&maps->tail, 4, Cpad + 4 * NG * plane, d2, s2, b2);
-    }
-    const cuuint64_t dims[4] = {(cuuint64_t)px, (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)nc};
-    const cuuint64_t strides[3] = {(cuuint64_t)px * 4, (cuuint64_t)px * ny * 4, plane * 4};
-    const cuuint32_t box[4] = {(cuuint32_t)CBX, (cuuint32_t)CBY, 1u, (cuuint32_t)nc};
-    cudaError_t e = encode_tiled(&maps->main, 4, Cpad, dims, strides, box);
-    maps->tail = maps->main;
-    return e;
-}
-
 cudaError_t launch_pad_stiffness(const float* C, float* Cpad, int nx, int ny, int nz, int nc, cudaStream_t s) {
     const int64_t px = zmarch_tma_pitch(nx);
-    if (nc == 21) {
-        const int64_t rows = (int64_t)nz * ny;
-        int64_t blocks = (rows * px + 255) / 256;
-        if (blocks > 152 * 16) blocks = 152 * 16;
-        k_pack_mm<<<(int)blocks, 256, 0, s>>>(C, Cpad, nx, (int)px, rows);
-        return cudaGetLastError();
-    }
     const int64_t rows = (int64_t)nc * nz * ny;
     int64_t blocks = (rows * px + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
@@ -559,7 +469,7 @@ cudaError_t launch_pad_stiffness(const float* C, float* Cpad, int nx, int ny, in
 }
 
 template <int SYM, int MODE>
-static cudaError_t zt_launch(const ZtMaps& maps, const float* x, const float* C, const LevelGeom<float>& G,
+static cudaError_t zt_launch(const CUtensorMap& map, const float* x, const float* C, const LevelGeom<float>& G,
                              const BcTable& bc, const float* b, const float* dg, float omega, float* out, int* err,
                              cudaStream_t s, cudaStream_t s_faces) {
     constexpr int NC = SYM == SYM_ISO ? 2 : 21;
@@ -583,11 +493,11 @@ static cudaError_t zt_launch(const ZtMaps& maps, const float* x, const float* C,
     k_zt_faces<SYM, MODE><<<fgrd, blk, 0, s_faces ? s_faces : s>>>(x, C, G, bc, b, dg, omega, out);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_zmarch_tma<SYM, MODE><<<grd, blk, bytes, s>>>(maps.main, maps.tail, x, G, b, dg, omega, out, kc, err);
+    k_zmarch_tma<SYM, MODE><<<grd, blk, bytes, s>>>(map, x, G, b, dg, omega, out, kc, err);
     return cudaGetLastError();
 }
 
-cudaError_t launch_zmarch_tma(int mode, int sym, const ZtMaps& map, const float* x, const float* C,
+cudaError_t launch_zmarch_tma(int mode, int sym, const CUtensorMap& map, const float* x, const float* C,
                               const LevelGeom<float>& G, const BcTable& bc, const float* b, const float* dg,
                               float omega, float* out, int* err, cudaStream_t s, cudaStream_t s_faces) {
     if (!zmarch_tma_supported(G.nx, G.ny, G.nz) || sym == SYM_MAJ) return cudaErrorInvalidValue;

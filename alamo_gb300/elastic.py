@@ -55,6 +55,8 @@ def default_opts(**kw):
             v = {"fp64": L.PRECISION_FP64, "mixed": L.PRECISION_MIXED}[v]
         if k == "solver" and isinstance(v, str):
             v = {"vcycle": L.SOLVER_VCYCLE, "fgmres": L.SOLVER_FGMRES}[v]
+        if k == "outer_residual" and isinstance(v, str):
+            v = {"fp64": L.OUTER_FP64, "dfloat": L.OUTER_DFLOAT}[v]
         if k == "smoother" and isinstance(v, str):
             v = {"jacobi": L.SMOOTHER_JACOBI, "gs": L.SMOOTHER_GS}[v]
         if k == "bottom_solver" and isinstance(v, str):
@@ -191,6 +193,18 @@ class Elastic:
         L.check(L.lib().agb_elastic_fsmooth(self.h, int(level), px, pb, int(ncalls), _same_where(wx, wb)))
         return x
 
+    def residual_dfloat(self, x, b, r=None):
+        """The fine-level residual in double-float arithmetic (FP64 arrays in
+        and out); returns (r, (inf-norm, 2-norm))."""
+        if r is None:
+            r = np.empty(self._vec_shape(0))
+        norms = (ctypes.c_double * 2)()
+        px, wx = _arg(x)
+        pb, wb = _arg(b)
+        pr, wr = _arg(r)
+        L.check(L.lib().agb_elastic_residual_dfloat(self.h, px, pb, pr, norms, _same_where(wx, wb, wr)))
+        return r, (norms[0], norms[1])
+
     def Fsmooth_f32(self, x, b, ncalls=1, level=0):
         """The mixed-precision cycle's FP32 Fsmooth, in place on x (float32)."""
         px, wx = _arg(x, np.float32)
@@ -322,6 +336,12 @@ class Elastic:
         ms = ctypes.c_double()
         L.check(L.lib().agb_profile_get(self.h, int(family), ctypes.byref(n), ctypes.byref(ms)))
         return n.value, ms.value
+
+    def profile_bytes(self, family):
+        """Algorithmic bytes of the family's timed launches since the reset."""
+        b = ctypes.c_double()
+        L.check(L.lib().agb_profile_bytes(self.h, int(family), ctypes.byref(b)))
+        return b.value
 
     def launch_count(self):
         n = ctypes.c_int64()

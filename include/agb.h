@@ -79,6 +79,15 @@ typedef enum { AGB_BOTTOM_BICGSTAB = 0, AGB_BOTTOM_DIRECT = 1, AGB_BOTTOM_SMOOTH
  * node colours (i & 1) + 2 (j & 1) + 4 (k & 1) in turn, in place; weight 1
  * on interior rows and opts.omega on boundary rows. */
 typedef enum { AGB_SMOOTHER_JACOBI = 0, AGB_SMOOTHER_GS = 1 } agb_smoother;
+/* The outer residual and solution update of the mixed-precision FGMRES
+ * solve.  AGB_OUTER_FP64: FP64 arithmetic (the reference's
+ * Operator<Grid::Node>::solutionResidual, src/Operator/Operator.cpp:635-657).
+ * AGB_OUTER_DFLOAT: double-float arithmetic on the FP32 pipe (each value the
+ * unevaluated sum of two floats, about 48 significant bits): the same
+ * operator and update with relative rounding near 1e-14 instead of 1e-16, at
+ * FP32 speed; the solution is returned in FP64.  Without psi only (psi runs
+ * the FP64 form). */
+typedef enum { AGB_OUTER_FP64 = 0, AGB_OUTER_DFLOAT = 1 } agb_outer_residual;
 
 /* Solver settings; field names follow the reference's `solver.*` keys
  * (Solver::Nonlocal::Linear::Parse, src/Solver/Nonlocal/Linear.H:296-382). */
@@ -111,6 +120,7 @@ typedef struct agb_solver_opts {
                                  ones a V-cycle; Linear::PrepareMLMG sets 100000000, so every
                                  iteration is an F-cycle (src/Solver/Nonlocal/Linear.H:261) (100000000) */
     int smoother;             /* agb_smoother: the Fsmooth of every level (AGB_SMOOTHER_JACOBI) */
+    int outer_residual;       /* agb_outer_residual of the mixed FGMRES solve (AGB_OUTER_FP64) */
 } agb_solver_opts;
 
 typedef struct agb_solve_report {
@@ -200,6 +210,12 @@ agb_status agb_elastic_residual(agb_elastic* h, int level, const double* x, cons
  * x, b, r: 3*N floats of that level. */
 agb_status agb_elastic_fsmooth_f32(agb_elastic* h, int level, float* x, const float* b, int ncalls, int where);
 agb_status agb_elastic_residual_f32(agb_elastic* h, int level, const float* x, const float* b, float* r, int where);
+/* The fine-level residual r = b - A x of agb_elastic_residual evaluated in
+ * double-float arithmetic (AGB_OUTER_DFLOAT: x, b and the stiffness as hi +
+ * lo FP32 pairs, FP32 instructions only), returned in FP64; the norms are
+ * those of r rounded to FP32.  No psi. */
+agb_status agb_elastic_residual_dfloat(agb_elastic* h, const double* x, const double* b, double* r, double norms[2],
+                                       int where);
 /* Operator<Grid::Node>::restriction (src/Operator/Operator.cpp:262-363):
  * fine field of level crse_level-1 -> coarse field of level crse_level */
 agb_status agb_elastic_restrict(agb_elastic* h, int crse_level, const double* fine, double* crse, int where);
@@ -358,12 +374,17 @@ typedef enum {
     AGB_K_RESTRICT = 6,
     AGB_K_PROLONG = 7,
     AGB_K_BOTTOM = 8,
-    AGB_K_NFAMILIES = 9
+    AGB_K_KRYLOV = 9,  /* FGMRES Gram-Schmidt: dots, projections, normalisation, e = Z y */
+    AGB_K_RESIDUAL_DF = 10, /* double-float outer residual of the mixed solve */
+    AGB_K_NFAMILIES = 11
 } agb_kernel_family;
 agb_status agb_profile_enable(agb_elastic* h, int on);
 agb_status agb_profile_reset(agb_elastic* h);
 /* launches and summed device milliseconds of one family since the reset */
 agb_status agb_profile_get(agb_elastic* h, int family, int64_t* launches, double* ms);
+/* algorithmic bytes (each vector read or written once per launch) of the
+ * timed launches of a family since the reset; kept for AGB_K_KRYLOV */
+agb_status agb_profile_bytes(agb_elastic* h, int family, double* bytes);
 /* kernels of this library launched since the handle was created */
 agb_status agb_launch_count(agb_elastic* h, int64_t* launches);
 

@@ -190,15 +190,16 @@ def test_fast_path_solution_vs_oracle_129_polycrystal(agb, oracle):
     refinement, direct 5^3 bottom) on a 129^3 cubic polycrystal under the
     uniaxial clamp, solved to 1e-10, against the oracle's FP64 solve
     (F-cycles, V(2,2), the exact 5^3 bottom: the reference's BiCGStab on the
-    singular 3^3 bottom of this BC stalls above 1e-12) to 1e-12: the
-    displacement within 1e-8 relative (inf-norm and 2-norm)."""
+    singular 3^3 bottom of this BC can stall) to 1e-10 (FP64 rounding of the
+    interior rows floors the relative residual near 1e-12 at this size):
+    the displacement within 1e-8 relative (inf-norm and 2-norm)."""
     from alamo_gb300 import workloads as W
     from alamo_gb300 import bc as B
     n = 129
     C, dx = W.voronoi_cubic(n, 64, seed=21)
     bc = B.TensionTest("uniaxial_stress_clamp", disp=0.01)
     u0, b, rhs, bt = newton_problem(agb, oracle, C, None, bc, dx)
-    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-12, max_iter=200, bottom_solver=1, max_coarsening_level=4)
+    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_iter=200, bottom_solver=1, max_coarsening_level=4)
     assert rep_o.status == 0
     with make_op(agb, C, bc, dx, precision=1, solver="fgmres", bottom_solver="direct", max_coarsening_level=4,
                  pre_smooth=1, post_smooth=1) as op:
@@ -673,4 +674,44 @@ def test_gs_vcycle_and_solve_parity(agb, oracle, case):
         u = u0.copy()
         rep = agb.Newton(op).solve(u, b, F0, tol_rel=1e-10, tol_abs=0.0)
     assert rep["status"] == 0
+    assert rel(u, xo) <= 1e-8
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_residual_dfloat_parity(agb, oracle, case):
+    """The double-float outer residual (hi + lo FP32 pairs, FP32
+    instructions only) against the oracle's FP64 residual
+    (Operator.cpp:635-657): within the FP64 bar of 1e-12 relative."""
+    C, F0, bc, dx = CASES[case]()
+    n = C.shape[0]
+    bt, _ = bc.tables()
+    x0 = P.random_field((3, n, n, n), 25)
+    b = P.random_field((3, n, n, n), 26)
+    with make_op(agb, C, bc, dx) as op:
+        r, (rinf, r2) = op.residual_dfloat(x0, b)
+    rr, rn = oracle.residual(C, bt, x0, b, dx)
+    assert rel(r, rr) <= TOL64
+    # the norms are those of r rounded to FP32
+    assert abs(rinf - rn) <= 1e-7 * rn
+    assert abs(r2 - np.sqrt((rr ** 2).sum())) <= 1e-7 * r2
+
+
+@pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
+def test_mixed_solve_dfloat_outer_residual(agb, oracle, case):
+    """The mixed FGMRES solve with the double-float outer residual and
+    update reaches the same solution as the oracle's FP64 solve, and its
+    FP64 residual (recomputed by the FP64 kernel) meets the tolerance."""
+    C, F0, bc, dx = CASES[case]()
+    n = C.shape[0]
+    mcl = oracle.num_levels(n, n, n) - 2
+    u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
+    xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_fmg_iter=0)
+    assert rep_o.status == 0
+    with make_op(agb, C, bc, dx, precision=1, solver="fgmres", bottom_solver="direct", max_coarsening_level=mcl,
+                 outer_residual="dfloat") as op:
+        u = u0.copy()
+        rep = agb.Newton(op).solve(u, b, F0, tol_rel=1e-10, tol_abs=0.0)
+        r64, (rinf, _) = op.residual(u, rhs)
+    assert rep["status"] == 0
+    assert rinf <= 1.5e-10 * np.abs(rhs).max()
     assert rel(u, xo) <= 1e-8
