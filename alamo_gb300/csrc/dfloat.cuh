@@ -34,9 +34,14 @@ __device__ __forceinline__ dfloat df_fast_two_sum(float a, float b) {
     return dfloat(s, b - (s - a), 0);
 }
 
+// The sum and the product leave their pair unnormalised (|lo| may reach a
+// few ulp(hi) instead of half of one): every operation below is exact in
+// its hi parts and takes the lo parts as small corrections, so a pair only
+// needs normalising where it leaves the arithmetic (df_value), and the
+// FastTwoSum of each step is saved (about a third of the instructions).
 __device__ __forceinline__ dfloat operator+(const dfloat& a, const dfloat& b) {
     const dfloat s = df_two_sum(a.hi, b.hi);
-    return df_fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+    return dfloat(s.hi, s.lo + (a.lo + b.lo), 0);
 }
 __device__ __forceinline__ dfloat operator-(const dfloat& a) { return dfloat(-a.hi, -a.lo, 0); }
 __device__ __forceinline__ dfloat operator-(const dfloat& a, const dfloat& b) { return a + (-b); }
@@ -45,8 +50,11 @@ __device__ __forceinline__ dfloat operator*(const dfloat& a, const dfloat& b) {
     float e = __fmaf_rn(a.hi, b.hi, -p);
     e = __fmaf_rn(a.hi, b.lo, e);
     e = __fmaf_rn(a.lo, b.hi, e);
-    return df_fast_two_sum(p, e);
+    return dfloat(p, e, 0);
 }
+// the pair's value rounded to FP32 / FP64
+__device__ __forceinline__ float df_float(const dfloat& a) { return a.hi + a.lo; }
+__device__ __forceinline__ double df_double(const dfloat& a) { return (double)a.hi + (double)a.lo; }
 __device__ __forceinline__ dfloat& operator+=(dfloat& a, const dfloat& b) { return a = a + b; }
 __device__ __forceinline__ dfloat& operator-=(dfloat& a, const dfloat& b) { return a = a - b; }
 __device__ __forceinline__ dfloat& operator*=(dfloat& a, const dfloat& b) { return a = a * b; }

@@ -67,8 +67,8 @@ __global__ void __launch_bounds__(256) k_residual_df(const dfloat* __restrict__ 
         for (int c = 0; c < 3; c++) {
             const int64_t q = c * G.N + id;
             const dfloat rv = b[q] - ax[c];
-            const float rf = rv.hi + rv.lo;
-            if (WIDE) r64[q] = (double)rv.hi + (double)rv.lo;
+            const float rf = df_float(rv);
+            if (WIDE) r64[q] = df_double(rv);
             else r[q] = rf;
             const double a = fabs((double)rf);
             // a NaN reaches the sum (the max drops it)
@@ -87,15 +87,18 @@ __global__ void k_to_df(const double* __restrict__ src, dfloat* __restrict__ dst
 
 __global__ void k_df_to_double(const dfloat* __restrict__ src, double* __restrict__ dst, int64_t n) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const dfloat v = src[q];
-        dst[q] = (double)v.hi + (double)v.lo;
+        dst[q] = df_double(src[q]);
     }
 }
 
 // x += a e, e an FP32 correction, a a double-float scale
 __global__ void k_df_axpy(const float* __restrict__ e, dfloat a, dfloat* __restrict__ x, int64_t n) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-        x[q] = x[q] + a * dfloat(e[q]);
+    {
+        // stored normalised: the iterate is updated many times
+        const dfloat v = x[q] + a * dfloat(e[q]);
+        x[q] = df_fast_two_sum(v.hi, v.lo);
+    }
 }
 
 __global__ void k_scale_f32(float* __restrict__ v, float a, int64_t n) {

@@ -379,6 +379,9 @@ def compare_fp64(A, torch, n, C, F0, bc, dx, net, name):
     xm, repm, secm = timed_solve(A, torch, n, C, F0, bc, dx, fast_opts(A, n), net=net, repeats=2)
     out = {"workload": name, "learned_mixed": rep_summary(repm, secm),
            "timing": "host wall clock around one synchronous C-ABI call, device-resident inputs"}
+    out["learned_mixed_gs_smoother"] = guarded(
+        lambda: rep_summary(*timed_solve(A, torch, n, C, F0, bc, dx, fast_opts(A, n, smoother="gs"), net=net,
+                                         repeats=2)[1:]))
     x64, rep64, sec64 = timed_solve(A, torch, n, C, F0, bc, dx, fp64_fgmres_opts(A, n))
     out["fp64_fgmres_direct_bottom"] = rep_summary(rep64, sec64)
     out["mixed_vs_fp64"] = rel_err(xm, x64)
@@ -645,6 +648,18 @@ def main():
             fp64_outer["solution_vs_fast_path"] = rel_err(u_fp64_outer, u_fast)
         except A.AgbError as e:
             fp64_outer = {"error": str(e)}
+    # the colour-ordered (multicolour Gauss-Seidel) smoother in place of
+    # damped Jacobi, same solver otherwise: cycles and time
+    gs_arm = None
+    if not args.no_plain and prec:
+        def gs_run():
+            ug, r, s = timed_solve(A, torch, n, C, F0, bc, dx, fast_opts(A, n, args, smoother="gs"), net=net,
+                                   repeats=2)
+            d = rep_summary(r, s)
+            d["solution_vs_fast_path"] = rel_err(ug, u_fast)
+            d["jacobi_cycles"] = reports[-1].get("iters") if reports else None
+            return d
+        gs_arm = guarded(gs_run)
     if not args.no_plain:
         try:
             u64, r, s = timed_solve(A, torch, n, C, F0, bc, dx, A.default_opts(precision=0))
@@ -743,6 +758,7 @@ def main():
                   "final_rel_resnorm": (rep.get("final_resnorm", 0) / rep["rhsnorm0"]) if rep else None,
                   "levels": rep.get("nlevels")},
         "plain_fp64": plain, "fp64_fgmres": fp64_fgmres, "fast_path_fp64_outer_residual": fp64_outer,
+        "fast_path_gs_smoother": gs_arm,
         "speedup_vs_plain_fp64": (plain["seconds"] / sec) if plain and "seconds" in plain else None,
         "fapply": fap, "kernels_in_timed_region": kernels, "other_configs": extra,
     }

@@ -283,7 +283,7 @@ def _f32_forms_vs_oracle(agb, oracle, C, bc, dx, seed):
     bt, _ = bc.tables()
     diag = oracle.diagonal(C, bt, dx)
     xs_ref = oracle.fsmooth(C, bt, diag, x.copy(), b, dx, ncalls=1)
-    r_ref = oracle.residual(C, bt, x, b, dx)
+    r_ref, _ = oracle.residual(C, bt, x, b, dx)
     with make_op(agb, C, bc, dx, fine_kernel=0) as op:
         xs = op.Fsmooth_f32(x.astype(np.float32), b.astype(np.float32), ncalls=1)
         r = op.residual_f32(x.astype(np.float32), b.astype(np.float32))

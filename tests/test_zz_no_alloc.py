@@ -66,7 +66,7 @@ def test_noalloc_matches_residual_entry_point(agb, oracle, case):
         assert abs(norms[0] - inf_ref) <= 1e-12 * inf_ref
         assert abs(norms[1] - l2_ref) <= 1e-12 * l2_ref
         # and the oracle's residual (Operator.cpp:635-657) on the same inputs
-        r_orc = oracle.residual(C, bt, x.cpu().numpy(), b.cpu().numpy(), dx)
+        r_orc, _ = oracle.residual(C, bt, x.cpu().numpy(), b.cpu().numpy(), dx)
         assert np.abs(rr - r_orc).max() <= 1e-12 * np.abs(r_orc).max()
         assert abs(norms[0] - np.abs(r_orc).max()) <= 1e-12 * np.abs(r_orc).max()
         assert abs(norms[1] - np.sqrt((r_orc ** 2).sum())) <= 1e-12 * np.sqrt((r_orc ** 2).sum())
