@@ -34,14 +34,14 @@ __device__ __forceinline__ dfloat df_fast_two_sum(float a, float b) {
     return dfloat(s, b - (s - a), 0);
 }
 
-// The sum and the product leave their pair unnormalised (|lo| may reach a
-// few ulp(hi) instead of half of one): every operation below is exact in
-// its hi parts and takes the lo parts as small corrections, so a pair only
-// needs normalising where it leaves the arithmetic (df_value), and the
-// FastTwoSum of each step is saved (about a third of the instructions).
+// The sum renormalises its pair (FastTwoSum): after cancellation of the hi
+// parts an unnormalised lo would be as large as hi, and a later product
+// would round it in single precision (measured: the 257^3 solve stalled
+// above 1e-8 without it).  The product leaves its pair unnormalised, |lo| a
+// few ulp(hi) at most, which the next operation absorbs.
 __device__ __forceinline__ dfloat operator+(const dfloat& a, const dfloat& b) {
     const dfloat s = df_two_sum(a.hi, b.hi);
-    return dfloat(s.hi, s.lo + (a.lo + b.lo), 0);
+    return df_fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
 }
 __device__ __forceinline__ dfloat operator-(const dfloat& a) { return dfloat(-a.hi, -a.lo, 0); }
 __device__ __forceinline__ dfloat operator-(const dfloat& a, const dfloat& b) { return a + (-b); }
