@@ -25,7 +25,8 @@ EXPORTS = [
     "agb_unet_create", "agb_unet_destroy", "agb_unet_num_params", "agb_unet_get_params", "agb_unet_set_params",
     "agb_unet_train_step", "agb_unet_predict", "agb_elastic_learned_guess", "agb_conv3_bf16",
     "agb_newton_solve_n", "agb_elastic_set_psi", "agb_newton_solve_guess", "agb_elastic_tensor",
-    "agb_newton_solve_neohookean",
+    "agb_newton_solve_neohookean", "agb_composite_create", "agb_composite_destroy", "agb_composite_level_dims",
+    "agb_composite_set_bc", "agb_composite_set_model", "agb_composite_solve",
 ]
 
 AGB_OK, AGB_NOT_CONVERGED, AGB_NAN, AGB_BAD_ARG, AGB_CUDA_ERROR, AGB_NOT_READY, AGB_OUT_OF_MEMORY, AGB_LIMIT = range(8)

@@ -22,8 +22,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-r
               "-Xptxas", "-warn-spills"] + ARCH
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 
-CU_SOURCES = ["kernels.cu", "bottom.cu", "zmarch_tma.cu", "noalloc.cu", "unet.cu", "residual_df.cu"]
-CXX_SOURCES = ["api.cpp", "synth.cpp", "unet.cpp"]
+CU_SOURCES = ["kernels.cu", "bottom.cu", "zmarch_tma.cu", "noalloc.cu", "unet.cu", "residual_df.cu", "composite.cu"]
+CXX_SOURCES = ["api.cpp", "synth.cpp", "unet.cpp", "composite.cpp"]
 
 
 def _run(cmd):

@@ -286,6 +286,39 @@ agb_status agb_newton_solve_neohookean(agb_elastic* h, const double* model, doub
  * gives 6 components (00, 11, 22, 12, 20, 01), else 9 row-major. */
 agb_status agb_elastic_tensor(agb_elastic* h, const double* u, int which, int voigt, double* out, int where);
 
+/* ------------------------------------------------ AMR composite solve */
+/* Solver::Nonlocal::Linear::solve on an AMR hierarchy (src/Solver/Nonlocal/
+ * Linear.H:131-168 driving amrex::MLMG over AMR levels), with the operator's
+ * hooks for it: reflux (src/Operator/Operator.cpp:526-633),
+ * fixUpResidualMask (:230-251) and averageDownCoeffsDifferentAmrLevels
+ * (src/Operator/Elastic.cpp:628-742).  Level 0: the domain, n0 nodes per
+ * axis, spacing dx0, the boundary conditions of agb_composite_set_bc.
+ * Level l >= 1 (refinement ratio 2): one box of nv[3 l + a] valid nodes
+ * from level index lo[3 l + a] (entries of level 0 ignored); lo even, nv
+ * odd, and the box with one ring of ghost nodes inside level l-1's valid
+ * nodes.  A fine level's arrays (stiffness, F0, solution) cover the box and
+ * its ghost ring: nv + 2 nodes per axis.  The solve runs the handle options'
+ * V-cycles on each level (precision FP64 or mixed) inside the composite
+ * iteration; it stops when the composite residual (every fine valid row and
+ * every coarse row not under a finer box) is within max(tol_abs, tol_rel x
+ * the composite right-hand side).  u: one array per level (output; ghost
+ * rings hold the interpolated coarse values). */
+typedef struct agb_composite agb_composite;
+agb_status agb_composite_create(agb_composite** c, int nlev, const int n0[3], const double dx0[3], int sym,
+                                const int* lo, const int* nv, const agb_solver_opts* opts);
+agb_status agb_composite_destroy(agb_composite* c);
+/* nodes per axis of a level's arrays */
+agb_status agb_composite_level_dims(agb_composite* c, int level, int dims[3]);
+/* the domain's boundary conditions (tables of agb_elastic_set_bc) */
+agb_status agb_composite_set_bc(agb_composite* c, const int* type, const double* val);
+/* the per-node stiffness of one level (AoS, as agb_elastic_set_model) */
+agb_status agb_composite_set_model(agb_composite* c, int level, const double* C, int where);
+/* F0: NULL or one eigenstrain array per level (NULL entries allowed),
+ * f0_ncomp 1 or 9; iters: composite iterations; relnorm: the final relative
+ * composite residual */
+agb_status agb_composite_solve(agb_composite* c, double* const* u, const double* const* F0, int f0_ncomp,
+                               double tol_rel, double tol_abs, int* iters, double* relnorm, int where);
+
 /* ------------------------------------------------ allocation-free call */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc:
  * a host code whose memory arena took the whole device at start-up, a plugin

@@ -63,6 +63,28 @@ ESHELBY_EPS = 0.1
 ESHELBY_EIGEN = 0.001
 
 
+def eshelby_fields(xs, ys=None, zs=None):
+    """Stiffness (lambda, mu per node) and dilatational eigenstrain of the
+    reference's Eshelby inclusion (see eshelby) at the nodes xs x ys x zs
+    (ys, zs default to xs)."""
+    from scipy.special import erf
+    ys = xs if ys is None else ys
+    zs = xs if zs is None else zs
+    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+    a = ESHELBY_AXES
+    q = (X / a[0]) ** 2 + (Y / a[1]) ** 2 + (Z / a[2]) ** 2
+    norm = np.sqrt((X / a[0] ** 2) ** 2 + (Y / a[1] ** 2) ** 2 + (Z / a[2] ** 2) ** 2)
+    del X, Y, Z
+    with np.errstate(divide="ignore", invalid="ignore"):
+        eta = 0.5 - 0.5 * erf((q - 1.0) / ESHELBY_EPS / norm)
+    eta[norm == 0.0] = 1.0
+    E, nu = ESHELBY_E, ESHELBY_NU
+    C = np.empty(eta.shape + (2,))
+    C[..., 0] = E * nu / (1 + nu) / (1 - 2 * nu)
+    C[..., 1] = E / 2 / (1 + nu)
+    return C, ESHELBY_EIGEN * eta
+
+
 def eshelby(n, half_width):
     """The reference's 3D Eshelby inclusion test (tests/Eshelby/input) on a
     uniform grid of n^3 nodes over [-half_width, half_width]^3: an ellipsoid
