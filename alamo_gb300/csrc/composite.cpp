@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -327,6 +328,7 @@ agb_status agb_composite_solve(agb_composite* c, double* const* u, const double*
             rn = std::fmax(rn, max_norm(c, v.r, v.n, l > 0, l + 1 < nl ? v.cov_dev : nullptr, 3));
             if (l + 1 < nl) CTRY(restrict_down(c, l, c->L[l + 1].r, v.r, 0));
         }
+        if (c->opts.verbose > 0) std::fprintf(stderr, "agb composite: iteration %d |r|/|b| = %.6e\n", it, rn / bn);
         if (std::isnan(rn)) { status = AGB_NAN; break; }
         if (rn <= target) { status = AGB_OK; break; }
         if (it >= maxit) break;
@@ -345,11 +347,11 @@ agb_status agb_composite_solve(agb_composite* c, double* const* u, const double*
             CCK(agb::launch_interp(p.c, p.n, p.off, v.c, v.n, v.off, 3, 1, s));
             CTRY(level_residual(c, l, v.c, v.r, v.t2));
             CTRY(level_vcycles(c, l, v.t2, v.t, fine_cycles));
-            CCK(agb::launch_interp(v.t, v.n, v.off, v.c, v.n, v.off, 3, 1, s));
+            CCK(agb::launch_axpy(1.0, v.t, v.c, 3 * v.N, s));
         }
         for (int l = 0; l < nl; l++) {
             Comp::Level& v = c->L[l];
-            CCK(agb::launch_interp(v.c, v.n, v.off, v.u, v.n, v.off, 3, 1, s));
+            CCK(agb::launch_axpy(1.0, v.c, v.u, 3 * v.N, s));
         }
     }
     // results

@@ -24,27 +24,31 @@ constexpr int DX = 32, DY = 4, DZ = 2;
 
 inline dim3 dgrid(int nx, int ny, int nz) { return dim3((nx + DX - 1) / DX, (ny + DY - 1) / DY, (nz + DZ - 1) / DZ); }
 
-__device__ __forceinline__ void blk_max_sum(double& mx, double& sm, double* out) {
+// block (max, sum) of per-thread FP32 values: warp shuffles in FP32 (the
+// FP64 pipe runs at 1/64 of the FP32 rate; a warp's 32 squares summed in
+// FP32 keep the 2-norm to about 1e-7, and the max is exact), then the
+// warps' results in FP64.  NaNs propagate.
+__device__ __forceinline__ void blk_max_sum_f(float mx, float sm, double* out) {
     __shared__ double smx[32], ssm[32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        const float y = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = (y > mx || y != y) ? y : mx;
         sm += __shfl_xor_sync(0xffffffffu, sm, o);
     }
     const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     const int nthr = blockDim.x * blockDim.y * blockDim.z;
     const int w = tid >> 5, l = tid & 31, nw = (nthr + 31) >> 5;
-    if (l == 0) { smx[w] = mx; ssm[w] = sm; }
+    if (l == 0) { smx[w] = (double)mx; ssm[w] = (double)sm; }
     __syncthreads();
-    if (w == 0) {
-        mx = (l < nw) ? smx[l] : 0.0;
-        sm = (l < nw) ? ssm[l] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            sm += __shfl_xor_sync(0xffffffffu, sm, o);
+    if (tid == 0) {
+        double m = 0.0, t = 0.0;
+        for (int q = 0; q < nw; q++) {
+            m = (smx[q] > m || smx[q] != smx[q]) ? smx[q] : m;
+            t += ssm[q];
         }
-        if (l == 0) { out[0] = mx; out[1] = sm; }
+        out[0] = m;
+        out[1] = t;
     }
 }
 
@@ -59,7 +63,7 @@ __global__ void __launch_bounds__(256) k_residual_df(const dfloat* __restrict__ 
     const int k = blockIdx.z * DZ + threadIdx.z;
     const bool live = (i < G.nx) & (j < G.ny) & (k < G.nz);
     const int64_t id = i + G.sy * j + G.sz * k;
-    double mx = 0.0, sm = 0.0;
+    float mx = 0.f, sm = 0.f;
     if (live) {
         dfloat ax[3];
         apply_node<dfloat, SYM, false>(x, C, G, bc, i, j, k, id, ax);
@@ -70,14 +74,13 @@ __global__ void __launch_bounds__(256) k_residual_df(const dfloat* __restrict__ 
             const float rf = df_float(rv);
             if (WIDE) r64[q] = df_double(rv);
             else r[q] = rf;
-            const double a = fabs((double)rf);
-            // a NaN reaches the sum (the max drops it)
-            mx = fmax(mx, a);
-            sm += a * a;
+            const float a = fabsf(rf);
+            mx = (a > mx || a != a) ? a : mx;
+            sm = __fmaf_rn(a, a, sm);
         }
     }
     const int blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    blk_max_sum(mx, sm, partials + 2 * blk);
+    blk_max_sum_f(mx, sm, partials + 2 * blk);
 }
 
 __global__ void k_to_df(const double* __restrict__ src, dfloat* __restrict__ dst, int64_t n) {

@@ -691,9 +691,10 @@ def test_residual_dfloat_parity(agb, oracle, case):
         r, (rinf, r2) = op.residual_dfloat(x0, b)
     rr, rn = oracle.residual(C, bt, x0, b, dx)
     assert rel(r, rr) <= TOL64
-    # the norms are those of r rounded to FP32
+    # the norms are those of r rounded to FP32 (squares summed in FP32
+    # within a warp)
     assert abs(rinf - rn) <= 1e-7 * rn
-    assert abs(r2 - np.sqrt((rr ** 2).sum())) <= 1e-7 * r2
+    assert abs(r2 - np.sqrt((rr ** 2).sum())) <= 1e-6 * r2
 
 
 @pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
