@@ -23,7 +23,7 @@ EXPORTS = [
     "agb_status_string",
     "agb_last_error", "agb_version", "agb_residual_norms_noalloc",
     "agb_unet_create", "agb_unet_destroy", "agb_unet_num_params", "agb_unet_get_params", "agb_unet_set_params",
-    "agb_unet_train_step", "agb_unet_predict", "agb_elastic_learned_guess", "agb_conv3_bf16",
+    "agb_unet_train_step", "agb_unet_predict", "agb_elastic_learned_guess", "agb_conv3_bf16", "agb_conv3_wgrad_bf16",
     "agb_newton_solve_n", "agb_elastic_set_psi", "agb_newton_solve_guess", "agb_elastic_tensor",
     "agb_newton_solve_neohookean", "agb_composite_create", "agb_composite_destroy", "agb_composite_level_dims",
     "agb_composite_set_bc", "agb_composite_set_model", "agb_composite_solve",

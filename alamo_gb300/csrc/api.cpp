@@ -930,8 +930,12 @@ agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, doub
 // computed on the fine FP32 level (the learned guess's fallback test); the
 // first refinement step starts from it instead of an FP64 residual, and
 // convergence is only declared on an FP64 residual
+// target_from_rhs: the relative tolerance refers to the right-hand side
+// alone (the solve from a learned guess must meet the tolerance of the
+// solve from zero), not to max(|rhs|, |r0|) as MLMG's test does
 agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_rel, double tol_abs,
-                     agb_solve_report* rep, bool x_zero = false, const float* r32_init = nullptr) {
+                     agb_solve_report* rep, bool x_zero = false, const float* r32_init = nullptr,
+                     bool target_from_rhs = false) {
     auto t0 = std::chrono::steady_clock::now();
     const bool mixed = h->opts.precision == AGB_PRECISION_MIXED;
     // the mixed solve needs the FP32 hierarchy and the fine FP64 stiffness
@@ -990,7 +994,7 @@ agb_status solve_dev(agb_elastic* h, double* x, const double* rhs, double tol_re
         fp64_res = 1;
     }
     const double resnorm0 = r[0];
-    const double max_norm = (bn[0] >= resnorm0) ? bn[0] : resnorm0;
+    const double max_norm = (target_from_rhs || bn[0] >= resnorm0) ? bn[0] : resnorm0;
     const double target = std::max(tol_abs, std::max(tol_rel, 1.e-16) * max_norm);
     const bool fixed = h->opts.fixed_iter > 0;
     const int maxit = fixed ? h->opts.fixed_iter : h->opts.max_iter;
@@ -1869,7 +1873,7 @@ agb_status agb_newton_solve_guess(agb_elastic* h, agb_unet* net, double* u, cons
     // a kept guess's FP32 residual (the fallback test's) starts the mixed
     // refinement; the FP64 residuals after each inner solve decide
     const float* r32 = (ok && h->opts.precision == AGB_PRECISION_MIXED) ? h->L32[0].rescor : nullptr;
-    const agb_status st = solve_dev(h, (double*)du, rhs0, tol_rel, tol_abs, rep, ok == 0, r32);
+    const agb_status st = solve_dev(h, (double*)du, rhs0, tol_rel, tol_abs, rep, ok == 0, r32, true);
     if (st != AGB_OK && st != AGB_NOT_CONVERGED) return st;
     TRY(finish_out(h, u, du, bytes, where));
     if (rep) rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

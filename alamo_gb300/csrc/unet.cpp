@@ -225,7 +225,8 @@ agb_status conv_back(agb_unet* net, int i, const __nv_bfloat16* x, const __nv_bf
     const int n = net->n[c.lvl];
     const int64_t V = net->V[c.lvl];
     cudaStream_t s = net->stream;
-    UCK(launch_conv_wgrad(x, c.cin, c.cin_real, net->gp[i], c.cout, n, n, n, net->G + c.off_w, net->G + c.off_b, s));
+    UCK(launch_conv_wgrad_tc(x, c.cin, c.cin_real, net->gp[i], c.cout, n, n, n, net->G + c.off_w, net->G + c.off_b,
+                             net->err, s));
     if (!gx) return AGB_OK;
     UCK(launch_grad_cast(net->gp[i], c.cout, 0, c.cout, nullptr, net->tmp, nullptr, V, s));
     UCK(launch_conv3(net->tmp, c.cout, c.Wd, nullptr, c.cin, n, n, n, 0, mask, nullptr, gx, net->err, s));
@@ -448,6 +449,30 @@ agb_status agb_conv3_bf16(const void* X, int Cin, const float* W, const float* b
     UCK(cudaStreamSynchronize(s));
     if (e) {
         set_last_error("a tensor-core wait of the convolution kernel did not complete in time");
+        return AGB_CUDA_ERROR;
+    }
+    return AGB_OK;
+}
+
+agb_status agb_conv3_wgrad_bf16(const void* X, int Cin, int CinW, const float* dY, int Cout, int nx, int ny, int nz,
+                                float* dW, float* db, int tensor_cores, void* stream) {
+    // test hook: dW [Cout][CinW][27] += sum_v dY[v][o] X[v + tap][c], db[o] += sum_v dY[v][o]
+    if (!X || !dY || !dW || !db || Cin % 16 || CinW > Cin) return AGB_BAD_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int* err = nullptr;
+    UCK(cudaMallocAsync((void**)&err, sizeof(int), s));
+    UCK(cudaMemsetAsync(err, 0, sizeof(int), s));
+    if (tensor_cores)
+        UCK(launch_conv_wgrad_tc(static_cast<const __nv_bfloat16*>(X), Cin, CinW, dY, Cout, nx, ny, nz, dW, db, err,
+                                 s));
+    else
+        UCK(launch_conv_wgrad(static_cast<const __nv_bfloat16*>(X), Cin, CinW, dY, Cout, nx, ny, nz, dW, db, s));
+    int e = 0;
+    UCK(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    UCK(cudaFreeAsync(err, s));
+    UCK(cudaStreamSynchronize(s));
+    if (e) {
+        set_last_error("a tensor-core wait of the weight-gradient kernel did not complete in time");
         return AGB_CUDA_ERROR;
     }
     return AGB_OK;

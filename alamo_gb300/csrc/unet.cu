@@ -243,6 +243,228 @@ cudaError_t conv_launch(const __nv_bfloat16* X, int Cin, const __nv_bfloat16* Wt
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradient of the 3x3x3 convolution on the tensor cores:
+//   dW[o][c][t] += sum_v dY[v][o] X[v + t][c],  db[o] += sum_v dY[v][o].
+// As a GEMM per CTA: D[m][o] = sum_k A[m][k] B[o][k] with the reduction over
+// the nodes k of the CTA's run of nodes; row m = (tap, channel) of one
+// 8-tap x 16-channel tile (M = 128), column o = output channel (N = Cout).
+// A[m][k] = X[node k shifted by tap][channel] (zero outside the grid),
+// B[o][k] = dY[node k][o] rounded to BF16.  Per stage of 64 nodes the CTA
+// gathers both operands into shared memory in the K-major no-swizzle layout
+// of the forward kernel (core matrices of 8 rows x 8 nodes; K halves LBO
+// apart, 8-row groups 128 bytes apart), one thread issues the stage's four
+// tcgen05.mma (K = 16 each) and commits to the stage buffer's mbarrier; two
+// buffers let the next gather overlap the MMAs.  The FP32 accumulator rows
+// are read back with tcgen05.ld and added into dW with atomics (the node runs
+// of different CTAs add up); the bias gradient is summed by the CTAs of the
+// first tile.
+constexpr int WT_STAGE_NODES = 64;  // nodes per stage (4 MMAs of K = 16)
+constexpr int WT_STAGES = 16;       // stages per CTA: 1024 nodes
+
+template <int N>
+struct WgCfg {
+    static constexpr int TMEM_COLS = ConvCfg<N>::TMEM_COLS;
+    static constexpr int A_KS = 128 * 16 * 2;  // bytes of A per 16-node K step
+    static constexpr int B_KS = N * 16 * 2;
+    static constexpr int A_ST = 4 * A_KS, B_ST = 4 * B_KS;
+    static constexpr int BUF = A_ST + B_ST;   // one stage buffer
+    static constexpr int SMEM = 2 * BUF + 128;
+};
+
+template <int N>
+__global__ void __launch_bounds__(128) k_wgrad_tc(const __nv_bfloat16* __restrict__ X, int Cin, int CinW,
+                                                  const float* __restrict__ dY, int nx, int ny, int nz,
+                                                  float* __restrict__ dW, float* __restrict__ db,
+                                                  int* __restrict__ err) {
+    using CFG = WgCfg<N>;
+    extern __shared__ unsigned char wg_raw[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    __shared__ float sdb[N];
+    const uint32_t raw = smem_u32(wg_raw);
+    const uint32_t pad = ((raw + 127u) & ~127u) - raw;
+    unsigned char* buf = wg_raw + pad;
+    const uint32_t buf_u32 = raw + pad;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t V = (int64_t)nx * ny * nz;
+    const int64_t v0 = (int64_t)blockIdx.x * (WT_STAGE_NODES * WT_STAGES);
+    const int tg = blockIdx.y & 3, cs = blockIdx.y >> 2;  // tap group (8 taps), 16-channel slice
+    const bool first_tile = blockIdx.y == 0;
+
+    if (tid == 0) {
+        abort_flag = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int q = tid; q < N; q += 128) sdb[q] = 0.f;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(CFG::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    constexpr uint32_t IDESC = idesc_bf16(128, N);
+
+    // gather one stage (nodes vs .. vs + 63) into buffer b
+    auto gather = [&](int st, int b) {
+        unsigned char* A = buf + b * CFG::BUF;
+        unsigned char* B = A + CFG::A_ST;
+        const int64_t vs = v0 + (int64_t)st * WT_STAGE_NODES;
+        // A: (local tap tl, node j) pairs, 16 channels each
+        for (int q = tid; q < 8 * WT_STAGE_NODES; q += 128) {
+            const int tl = q / WT_STAGE_NODES, j = q - tl * WT_STAGE_NODES;
+            const int t = tg * 8 + tl;
+            const int64_t v = vs + j;
+            uint4 lo4 = make_uint4(0, 0, 0, 0), hi4 = make_uint4(0, 0, 0, 0);
+            if (t < 27 && v < V) {
+                const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((int64_t)nx * ny));
+                const int xx = x + t % 3 - 1, yy = y + (t / 3) % 3 - 1, zz = z + t / 9 - 1;
+                if (xx >= 0 && xx < nx && yy >= 0 && yy < ny && zz >= 0 && zz < nz) {
+                    const uint4* src = reinterpret_cast<const uint4*>(
+                        X + (xx + (int64_t)nx * (yy + (int64_t)ny * zz)) * Cin + cs * 16);
+                    lo4 = src[0];
+                    hi4 = src[1];
+                }
+            }
+            const __nv_bfloat16* e0 = reinterpret_cast<const __nv_bfloat16*>(&lo4);
+            const __nv_bfloat16* e1 = reinterpret_cast<const __nv_bfloat16*>(&hi4);
+            const int ks = j >> 4, kh = (j >> 3) & 1, e = j & 7;
+            unsigned char* base = A + ks * CFG::A_KS + e * 2;
+#pragma unroll
+            for (int c = 0; c < 16; c++) {
+                const int m = tl * 16 + c;
+                *reinterpret_cast<__nv_bfloat16*>(base + (kh * 16 + (m >> 3)) * 128 + (m & 7) * 16) =
+                    c < 8 ? e0[c] : e1[c - 8];
+            }
+        }
+        // B: (node j, group of 8 output channels)
+        for (int q = tid; q < WT_STAGE_NODES * (N / 8); q += 128) {
+            const int j = q / (N / 8), g = q - j * (N / 8);
+            const int64_t v = vs + j;
+            float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (v < V) {
+                const float4* src = reinterpret_cast<const float4*>(dY + v * N + g * 8);
+                const float4 a = src[0], bb = src[1];
+                f[0] = a.x; f[1] = a.y; f[2] = a.z; f[3] = a.w;
+                f[4] = bb.x; f[5] = bb.y; f[6] = bb.z; f[7] = bb.w;
+                if (first_tile) {
+#pragma unroll
+                    for (int i = 0; i < 8; i++) atomicAdd(&sdb[g * 8 + i], f[i]);
+                }
+            }
+            const int ks = j >> 4, kh = (j >> 3) & 1, e = j & 7;
+            unsigned char* base = B + ks * CFG::B_KS + (kh * (N / 8) + g) * 128 + e * 2;
+#pragma unroll
+            for (int i = 0; i < 8; i++) *reinterpret_cast<__nv_bfloat16*>(base + i * 16) = __float2bfloat16(f[i]);
+        }
+    };
+    auto issue = [&](int st, int b) {  // one thread
+        const uint32_t a_u32 = buf_u32 + b * CFG::BUF;
+        const uint32_t b_u32 = a_u32 + CFG::A_ST;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int ks = 0; ks < 4; ks++) {
+            const uint64_t ad = sdesc(a_u32 + ks * CFG::A_KS, 16 * 128, 128);
+            const uint64_t bd = sdesc(b_u32 + ks * CFG::B_KS, (N / 8) * 128, 128);
+            const uint32_t acc = (st > 0 || ks > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+                : "memory");
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(&bars[b]))
+                     : "memory");
+    };
+
+    int nst = 0;
+    for (int st = 0; st < WT_STAGES; st++) {
+        if (v0 + (int64_t)st * WT_STAGE_NODES >= V) break;
+        const int b = st & 1;
+        if (st >= 2) {
+            // the MMAs of stage st - 2 read this buffer
+            if (tid == 0 && !mbar_wait(smem_u32(&bars[b]), (uint32_t)(((st - 2) >> 1) & 1))) {
+                abort_flag = 1;
+                if (err) atomicExch(err, 1);
+            }
+            __syncthreads();
+            if (abort_flag) break;
+        }
+        gather(st, b);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) issue(st, b);
+        nst = st + 1;
+    }
+    // the last stage's commit covers every MMA issued before it; waited for
+    // (bounded) after an abort too, before the accumulator is freed
+    if (nst > 0 && tid == 0) {
+        const int last = nst - 1;
+        if (!mbar_wait(smem_u32(&bars[last & 1]), (uint32_t)((last >> 1) & 1))) {
+            abort_flag = 1;
+            if (err) atomicExch(err, 1);
+        }
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (nst > 0 && !abort_flag) {
+        const int m = warp * 32 + lane;
+        const int tl = m >> 4, c = cs * 16 + (m & 15), t = tg * 8 + tl;
+        const bool live = t < 27 && c < CinW;
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            uint32_t r[16];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (live) {
+#pragma unroll
+                for (int jj = 0; jj < 16; jj++)
+                    atomicAdd(&dW[((int64_t)(c0 + jj) * CinW + c) * 27 + t], __uint_as_float(r[jj]));
+            }
+        }
+        if (first_tile)
+            for (int q = tid; q < N; q += 128) atomicAdd(&db[q], sdb[q]);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(CFG::TMEM_COLS)
+                     : "memory");
+}
+
+template <int N>
+cudaError_t wgrad_launch(const __nv_bfloat16* X, int Cin, int CinW, const float* dY, int nx, int ny, int nz,
+                         float* dW, float* db, int* err, cudaStream_t s) {
+    constexpr int bytes = WgCfg<N>::SMEM;
+    static bool configured[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64 || !configured[dev]) {
+        e = cudaFuncSetAttribute(k_wgrad_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        if (dev >= 0 && dev < 64) configured[dev] = true;
+    }
+    const int64_t V = (int64_t)nx * ny * nz;
+    const int64_t per = (int64_t)WT_STAGE_NODES * WT_STAGES;
+    dim3 grd((unsigned)((V + per - 1) / per), 4 * (Cin / 16), 1);
+    k_wgrad_tc<N><<<grd, 128, bytes, s>>>(X, Cin, CinW, dY, nx, ny, nz, dW, db, err);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t launch_conv3(const __nv_bfloat16* X, int Cin, const __nv_bfloat16* Wt, const float* bias, int Cout,
@@ -573,6 +795,20 @@ cudaError_t launch_conv_wgrad(const __nv_bfloat16* X, int Cin, int CinW, const f
     dim3 grd((unsigned)((V + WG_NODES - 1) / WG_NODES), (CinW + 15) / 16, Cout / 16);
     k_wgrad<<<grd, 256, 0, s>>>(X, Cin, CinW, dY, Cout, nx, ny, nz, dW, db);
     return cudaGetLastError();
+}
+cudaError_t launch_conv_wgrad_tc(const __nv_bfloat16* X, int Cin, int CinW, const float* dY, int Cout, int nx, int ny,
+                                 int nz, float* dW, float* db, int* err, cudaStream_t s) {
+    if (Cin <= 0 || Cin % 16 || CinW > Cin || nx < 1 || ny < 1 || nz < 1) return cudaErrorInvalidValue;
+    switch (Cout) {
+        case 16: return wgrad_launch<16>(X, Cin, CinW, dY, nx, ny, nz, dW, db, err, s);
+        case 32: return wgrad_launch<32>(X, Cin, CinW, dY, nx, ny, nz, dW, db, err, s);
+        case 48: return wgrad_launch<48>(X, Cin, CinW, dY, nx, ny, nz, dW, db, err, s);
+        case 64: return wgrad_launch<64>(X, Cin, CinW, dY, nx, ny, nz, dW, db, err, s);
+        case 96: return wgrad_launch<96>(X, Cin, CinW, dY, nx, ny, nz, dW, db, err, s);
+        case 128: return wgrad_launch<128>(X, Cin, CinW, dY, nx, ny, nz, dW, db, err, s);
+        case 192: return wgrad_launch<192>(X, Cin, CinW, dY, nx, ny, nz, dW, db, err, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 cudaError_t launch_down_bf16(const __nv_bfloat16* X, int nx, int ny, int nz, int C, __nv_bfloat16* Y, int mx, int my,
                              int mz, float s, cudaStream_t st) {

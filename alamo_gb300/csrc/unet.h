@@ -29,6 +29,10 @@ cudaError_t launch_pack_conv_dgrad(const float* W, int Cout, int Cin, __nv_bfloa
 // db[o] += sum_v dY[v][o]
 cudaError_t launch_conv_wgrad(const __nv_bfloat16* X, int Cin, int CinW, const float* dY, int Cout, int nx, int ny,
                               int nz, float* dW, float* db, cudaStream_t s);
+// the same on the tensor cores (tcgen05.mma, BF16 operands, FP32
+// accumulation; dY rounded to BF16); *err = 1 if a tensor-core wait gave up
+cudaError_t launch_conv_wgrad_tc(const __nv_bfloat16* X, int Cin, int CinW, const float* dY, int Cout, int nx, int ny,
+                                 int nz, float* dW, float* db, int* err, cudaStream_t s);
 // nodal full-weighting down-sampling to (mx, my, mz) = ((n - 1) / 2 + 1) and
 // trilinear up-sampling, channels-last, scaled by s (the adjoint of one is
 // the other times 8 or 1/8)

@@ -384,7 +384,10 @@ agb_status agb_elastic_learned_guess(agb_elastic* h, agb_unet* net, const double
  * solve, in one call: agb_elastic_learned_guess then agb_linear_solve on
  * device data, so host callers copy b (and F0) in and u out once.  u is
  * output only (the step starts from zero); used (may be NULL) reports
- * whether the guess was kept. */
+ * whether the guess was kept.  The solve stops at max(tol_abs, tol_rel
+ * |rhs|_inf): the tolerance of the solve from zero, whatever the residual at
+ * the guess (MLMG's max(|rhs|, |r0|) would loosen it after a guess whose
+ * residual exceeds |rhs|). */
 agb_status agb_newton_solve_guess(agb_elastic* h, agb_unet* net, double* u, const double* b, const double* F0,
                                   int f0_ncomp, double tol_rel, double tol_abs, agb_solve_report* rep, int* used,
                                   int where);
@@ -393,6 +396,13 @@ agb_status agb_newton_solve_guess(agb_elastic* h, agb_unet* net, double* u, cons
  * Y (BF16) or Yf (FP32), exactly one non-NULL; stream may be NULL. */
 agb_status agb_conv3_bf16(const void* X, int Cin, const float* W, const float* bias, int Cout, int nx, int ny, int nz,
                           int relu, void* Y, float* Yf, void* stream);
+/* Test hook of the convolution's weight gradient: dW [Cout][CinW][27] (FP32)
+ * += sum_v dY[v][o] X[v + tap][c] and db [Cout] += sum_v dY[v][o], X [V][Cin]
+ * BF16 channels-last, dY [V][Cout] FP32 (device pointers); tensor_cores != 0
+ * runs the tcgen05 kernel the training uses (dY rounded to BF16), 0 the FP32
+ * CUDA-core kernel; stream may be NULL. */
+agb_status agb_conv3_wgrad_bf16(const void* X, int Cin, int CinW, const float* dY, int Cout, int nx, int ny, int nz,
+                                float* dW, float* db, int tensor_cores, void* stream);
 
 /* --------------------------------------------------------- profiling */
 /* Kernel families timed with CUDA events on the handle's stream when

@@ -58,6 +58,39 @@ def test_conv3_matches_torch(agb, cin, cout, dims):
     assert (Yb.float() - ref).abs().max().item() <= 8e-3 * ref.abs().max().item()
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("cin,cinw,cout,dims", [(16, 16, 16, (13, 21, 9)), (32, 32, 64, (8, 16, 3)),
+                                                (48, 48, 16, (17, 17, 17)), (192, 192, 64, (9, 9, 9)),
+                                                (16, 3, 16, (11, 5, 7)), (96, 96, 32, (33, 9, 5)),
+                                                (64, 64, 128, (9, 9, 9)), (128, 128, 48, (5, 6, 7)),
+                                                (16, 16, 192, (7, 7, 7))])
+def test_conv3_weight_gradient_matches_torch(agb, cin, cinw, cout, dims):
+    """The convolution's weight and bias gradients, tensor-core kernel
+    (training) and CUDA-core kernel, against PyTorch's conv3d_weight in FP32:
+    the tensor-core kernel takes dY rounded to BF16, so its reference does
+    too; both accumulate into dW / db (here from zero)."""
+    dev = torch.device("cuda", 0)
+    nx, ny, nz = dims
+    g = torch.Generator().manual_seed(cin * 7 + cout)
+    X = _bf16(torch.randn(nz, ny, nx, cin, generator=g))
+    X[..., cinw:] = 0.0
+    X = X.to(dev)
+    dY = torch.randn(nz, ny, nx, cout, generator=g).to(dev)
+    Xb = X.to(torch.bfloat16).contiguous()
+    xin = X[..., :cinw].permute(3, 0, 1, 2)[None]
+    for tc in (1, 0):
+        dW = torch.zeros(cout, cinw, 27, device=dev)
+        db = torch.zeros(cout, device=dev)
+        st = agb.lib().agb_conv3_wgrad_bf16(ctypes.c_void_p(Xb.data_ptr()), cin, cinw, ctypes.c_void_p(dY.data_ptr()),
+                                            cout, nx, ny, nz, ctypes.c_void_p(dW.data_ptr()),
+                                            ctypes.c_void_p(db.data_ptr()), tc, None)
+        assert st == 0, agb.last_error()
+        go = (_bf16(dY) if tc else dY).permute(3, 0, 1, 2)[None]
+        ref = torch.nn.grad.conv3d_weight(xin, (cout, cinw, 3, 3, 3), go, padding=1).reshape(cout, cinw, 27)
+        assert (dW - ref).abs().max().item() <= 1e-4 * ref.abs().max().item()
+        assert (db - dY.sum(dim=(0, 1, 2))).abs().max().item() <= 1e-4 * dY.abs().sum(dim=(0, 1, 2)).max().item()
+
+
 def test_conv3_rejects_bad_shapes(agb):
     null = ctypes.c_void_p(16)
     assert agb.lib().agb_conv3_bf16(null, 12, null, None, 16, 4, 4, 4, 0, null, None, None) != 0
