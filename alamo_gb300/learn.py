@@ -208,8 +208,10 @@ def train(net, feats, sols, epochs=3, lr=1e-3, lr_end=1e-4, seed=0, log=None):
 
 def guess_and_solve(n, C, F0, bc, dx, net=None, tol=1e-8, sym="isotropic"):
     """Mixed FGMRES Newton solve of one medium from the learned guess (net
-    given) or from zero; returns (u, report, seconds, guess info).  Times the
-    whole call on the host, guess included (GPU work is synchronous)."""
+    given, agb_newton_solve_guess: the guess, its fallback and the solve to
+    the zero-start tolerance in one call) or from zero; returns (u, report,
+    seconds, guess info).  Times the whole call on the host, guess included
+    (GPU work is synchronous)."""
     import time
     nlev = _levels(n)
     o = default_opts(precision="mixed", solver="fgmres", bottom_solver="direct", max_coarsening_level=max(nlev - 2, 0))
@@ -218,15 +220,13 @@ def guess_and_solve(n, C, F0, bc, dx, net=None, tol=1e-8, sym="isotropic"):
         op.SetBC(bc)
         b = op.bc_init()
         op.prepareForSolve()
+        u = np.zeros((3, n, n, n))
         t0 = time.perf_counter()
         info = None
         if net is not None:
-            u, rhs, norms, used = learned_guess(op, net, b, F0)
-            info = {"used": used, "restricted_residual_guess": norms[0], "restricted_residual_zero": norms[1],
-                    "guess_s": time.perf_counter() - t0}
-            rep = Linear(op).solve(u, rhs, tol, 0.0, allow_not_converged=True)
+            rep = Newton(op).solve_guess(net, u, b, F0, tol_rel=tol, tol_abs=0.0, allow_not_converged=True)
+            info = {"used": rep["guess_used"]}
         else:
-            u = np.zeros((3, n, n, n))
             rep = Newton(op).solve(u, b, F0, tol_rel=tol, tol_abs=0.0, allow_not_converged=True)
         sec = time.perf_counter() - t0
     return u, rep, sec, info
