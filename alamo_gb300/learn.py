@@ -11,13 +11,14 @@ inclusion media (count 1-40, radius U[0.03, 0.15], contrast log-U[1, 20],
 eigenstrain U[0, 0.02], zero-displacement faces), generated here on the GPU.
 """
 import ctypes
+import os
 
 import numpy as np
 
 from . import _lib as L
 from . import bc as B
 from . import synth
-from .elastic import DevicePtr, Elastic, Linear, Newton, _arg, _same_where, default_opts
+from .elastic import DevicePtr, Elastic, Newton, _arg, _same_where, default_opts
 
 
 class UNet:
@@ -232,6 +233,10 @@ def guess_and_solve(n, C, F0, bc, dx, net=None, tol=1e-8, sym="isotropic"):
     return u, rep, sec, info
 
 
+# the trained 65^3 network shipped with the package
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "unet65.npy")
+
+
 def _main():
     import argparse
     import json
@@ -246,10 +251,10 @@ def _main():
     tr.add_argument("--seed", type=int, default=1)
     tr.add_argument("--out", required=True)
     pr = sub.add_parser("predict", help="time the network on one inclusion medium of its grid")
-    pr.add_argument("--weights", required=True)
+    pr.add_argument("--weights", default=WEIGHTS)
     pr.add_argument("--repeat", type=int, default=10)
     ev = sub.add_parser("evaluate")
-    ev.add_argument("--weights", required=True)
+    ev.add_argument("--weights", default=WEIGHTS)
     ev.add_argument("--n", type=int, default=129)
     ev.add_argument("--count", type=int, default=5)
     ev.add_argument("--seed", type=int, default=1000003)

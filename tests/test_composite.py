@@ -4,10 +4,10 @@ reference's two AMR known answers:
 
 - tests/UniaxialTension (three levels, a linear displacement and a constant
   stress, relative squared error < 1e-8);
-- tests/Eshelby (AMR around the inclusion; displacement and normal stress
-  along x = y = 0.25 within 0.1 of the analytic solution), here with three
-  levels: 65^3 over [-8, 8]^3 and two boxes of 63^3 valid nodes at spacings
-  1/8 and 1/16.
+- tests/Eshelby (four levels around the inclusion; displacement and normal
+  stress along x = y = 0.25 within 0.1 of the analytic solution): 65^3 over
+  [-8, 8]^3 and boxes of 63^3, 63^3 and 95^3 valid nodes at spacings 1/8,
+  1/16 and 1/32.
 
 The GPU tests compare the library's composite solution with the oracle's
 (the same iteration in FP64) and repeat the known-answer gates on it.
@@ -47,19 +47,21 @@ def uniaxial_levels():
     return 33, dx0, boxes, Cs, [None] * 3, bc, E
 
 
-def eshelby_levels():
-    """tests/Eshelby on [-8, 8]^3: level 0 65^3 (spacing 1/4), boxes of 63
-    valid nodes from -4 (spacing 1/8) and from -2 (spacing 1/16)."""
+def eshelby_levels(nvs=(63, 63, 95)):
+    """tests/Eshelby on [-8, 8]^3 with four levels: level 0 65^3 (spacing
+    1/4) and boxes about the origin of 63 valid nodes from -4 (spacing 1/8),
+    63 from -2 (1/16) and 95 from -1.5 (1/32).  The finest box's faces lie
+    outside the inclusion's diffuse boundary (semi-axes 1, 0.75, 0.5, width
+    0.1), as the reference's gradient tagging keeps them."""
     n0, hw = 65, 8.0
     dx0 = 2 * hw / (n0 - 1)
     xs = -hw + dx0 * np.arange(n0)
     C0, F00 = P.eshelby_fields(xs)
     Cs, F0s, boxes = [C0], [F00], []
-    for l in (1, 2):
+    for l, nv in enumerate(nvs, start=1):
         h = dx0 / 2 ** l
-        lo = int(round((hw - hw / 2 ** l) / h))
+        lo = int(round((hw - h * (nv - 1) / 2) / h))
         lo -= lo % 2
-        nv = 63
         c = -hw + h * (lo - 1 + np.arange(nv + 2))
         C, F0 = P.eshelby_fields(c)
         Cs.append(C)
