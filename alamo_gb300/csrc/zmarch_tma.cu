@@ -11,12 +11,18 @@
 //     derivatives of C) and of plane k+1 at the block's own columns (for
 //     the z-derivative): a 3-slot ring of TMA boxes (36 x 10 nodes x NC
 //     entries), plane k+2 issued at the top of step k into the slot plane
-//     k-1 has left; the stiffness of plane k-1 at the own column is kept in
-//     registers from the previous step.
-// Everything the stencil reads then comes from shared memory at offsets that
-// are compile-time constants, and each array is read from HBM about once per
-// sweep.  The six boundary faces (2.3% of the nodes at 257^3) run in a
-// second, thin kernel: inside the marching blocks their branchy rows held
+//     k-1 has left.
+// In the major-minor kernel, what a column needs again one plane later
+// stays in its registers: the own-column stiffness of planes k-1 and k, and
+// the displacement of planes k-1 and k at the column and its four in-plane
+// axis neighbours.  A step then reads from shared memory the stiffness of
+// plane k at the four in-plane neighbours and of plane k+1 at the column,
+// plane k+1's five displacement points and plane k's four in-plane
+// diagonals: 108 values per node instead of 153, at offsets that are
+// compile-time constants.  The isotropic kernel carries only the own-column
+// stiffness of plane k-1.  Each array is read from HBM about once per sweep.
+// The six boundary faces (2.3% of the nodes at 257^3) run in a second, thin
+// kernel: inside the marching blocks their branchy rows held
 // every step of the edge tiles back at the block barrier.  The TMA box
 // starts at x = x0 - 1 = 32 * blockIdx.x, a multiple of 4 floats (16 bytes);
 // the stiffness copy it reads has its x pitch padded to a multiple of 4
@@ -50,9 +56,8 @@ constexpr int CBX = 36, CBY = 10;                 // TMA box (x, y) of a stiffne
 constexpr int CEL = CBX * CBY;                    // floats per stiffness entry in a slot
 constexpr uint64_t WAIT_NS = 1000000000ull;       // 1 s: a TMA load takes microseconds
 
-// Prefetch distance and ring sizes.  Step k reads planes k-1 (displacement;
-// its own-column stiffness is in registers), k and k+1, and issues plane
-// k+1+DIST; plane k+DIST must have landed before step k+1.  The isotropic
+// Prefetch distance and ring sizes.  Step k reads planes k and k+1 (plane
+// k-1 is in registers), and issues plane k+1+DIST; plane k+DIST must have landed before step k+1.  The isotropic
 // planes are small (2 stiffness entries), so one plane of work does not
 // cover a load's latency: they look two planes ahead.  The major-minor
 // planes (21 entries) cover it with one, and two would not fit two blocks
@@ -122,8 +127,9 @@ __device__ __forceinline__ void cp_async_wait_group() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// isotropic: three blocks per SM (at most 85 registers), major-minor: two
 template <int SYM, int MODE>
-__global__ void __launch_bounds__(NT, 2)
+__global__ void __launch_bounds__(NT, SYM == SYM_ISO ? 3 : 2)
     k_zmarch_tma(const __grid_constant__ CUtensorMap cmap, const float* __restrict__ x, LevelGeom<float> G,
                  const float* __restrict__ b, const float* __restrict__ dg, float omega, float* __restrict__ out,
                  int kchunk, int* __restrict__ err) {
@@ -228,11 +234,40 @@ __global__ void __launch_bounds__(NT, 2)
     }
     cp_async_wait_group<DIST - 1>();
     __syncthreads();
-    float Cp[NC];
+    // carried from step to step in registers: the own column's stiffness of
+    // plane k-1 and, in the major-minor kernel (ZC), of plane k and the
+    // displacement of planes k-1 and k at the column and its four in-plane
+    // axis neighbours (each step then reads plane k+1's five points and
+    // plane k's four in-plane diagonals).  Measured at 257^3: +1.3 % on the
+    // major-minor sweep, whose 21 stiffness entries dominate the shared
+    // loads; -1.3 % on the isotropic one, which is issue bound and pays
+    // more for the register copies than it saves in loads.
+    constexpr bool ZC = SYM == SYM_MM;
+    constexpr int PL = UHY * UHX;
+    float Cp[NC], Cc[NC], Um[3][5], Uc[3][5];
+    auto load5 = [&](const float* s, float v[3][5]) {
+#pragma unroll
+        for (int p = 0; p < 3; p++) {
+            v[p][0] = s[p * PL];
+            v[p][1] = s[p * PL + 1];
+            v[p][2] = s[p * PL - 1];
+            v[p][3] = s[p * PL + UHX];
+            v[p][4] = s[p * PL - UHX];
+        }
+    };
     {
         const float* c = cslot(k0 - 1);
+        const float* cz = cslot(k0);
 #pragma unroll
-        for (int e = 0; e < NC; e++) Cp[e] = c[e * CEL];
+        for (int e = 0; e < NC; e++) {
+            Cp[e] = c[e * CEL];
+            Cc[e] = cz[e * CEL];
+        }
+        if (ZC) {
+            const int o = (ty + 1) * UHX + (tx + 1);
+            load5(Us + ((k0 - 1) % US) * UPL + o, Um);
+            load5(Us + (k0 % US) * UPL + o, Uc);
+        }
     }
     // the first step reloads the slot of plane k0 - 1: everyone has read it
     __syncthreads();
@@ -293,19 +328,43 @@ __global__ void __launch_bounds__(NT, 2)
             const float* u0 = Us + su * UPL + o;
             const float* um = Us + wrap(su + US - 1, US) * UPL + o;
             const float* up = Us + wrap(su + 1, US) * UPL + o;
-            auto U = [&](int p, int a, int bb, int c) -> float {
-                const float* s = c == 0 ? u0 : (c < 0 ? um : up);
-                return s[p * (UHY * UHX) + bb * UHX + a];
-            };
-            // the own column's stiffness of plane k, read once: the stencil's
-            // centre entries and, for the next step, the plane-below values
-            float c0[NC];
+            // ZC: plane k+1's five points (kept for the next step), every
+            // stiffness entry of its own column (the next step's centre) and
+            // plane k's in-plane diagonals; otherwise the own column of plane
+            // k, and the displacement is read where the stencil needs it
+            float Up[3][5], Cn[NC], Ud[3][4];
+            if (ZC) {
+                load5(up, Up);
 #pragma unroll
-            for (int e = 0; e < NC; e++) c0[e] = cc[e * CEL];
+                for (int e = 0; e < NC; e++) Cn[e] = cn[e * CEL];
+#pragma unroll
+                for (int p = 0; p < 3; p++) {
+                    Ud[p][0] = u0[p * PL + UHX + 1];
+                    Ud[p][1] = u0[p * PL - UHX - 1];
+                    Ud[p][2] = u0[p * PL - UHX + 1];
+                    Ud[p][3] = u0[p * PL + UHX - 1];
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < NC; e++) Cc[e] = cc[e * CEL];
+            }
+            // (a, bb) with at most one non-zero: 0 centre, 1 +x, 2 -x, 3 +y, 4 -y;
+            // both non-zero: the diagonals (1,1), (-1,-1), (1,-1), (-1,1)
+            auto U = [&](int p, int a, int bb, int c) -> float {
+                if (!ZC) {
+                    const float* s = c == 0 ? u0 : (c < 0 ? um : up);
+                    return s[p * PL + bb * UHX + a];
+                }
+                const int q5 = a == 1 ? 1 : (a == -1 ? 2 : (bb == 1 ? 3 : (bb == -1 ? 4 : 0)));
+                if (c < 0) return Um[p][q5];
+                if (c > 0) return Up[p][q5];
+                if (a != 0 && bb != 0) return Ud[p][a == bb ? (a > 0 ? 0 : 1) : (a > 0 ? 2 : 3)];
+                return Uc[p][q5];
+            };
             auto Cf = [&](int e, int a, int bb, int c) -> float {
-                if (c > 0) return cn[e * CEL];
+                if (c > 0) return ZC ? Cn[e] : cn[e * CEL];
                 if (c < 0) return Cp[e];
-                if (a == 0 && bb == 0) return c0[e];
+                if (a == 0 && bb == 0) return Cc[e];
                 return cc[e * CEL + bb * CBX + a];
             };
             float r[3];
@@ -316,14 +375,26 @@ __global__ void __launch_bounds__(NT, 2)
                 if (MODE == 0) {
                     out[q] = r[c];
                 } else if (MODE == 1) {
-                    const float xv = u0[c * (UHY * UHX)];
+                    const float xv = ZC ? Uc[c][0] : u0[c * PL];
                     out[q] = xv + omega * (bq[c] - r[c]) * dq[c];
                 } else {
                     out[q] = bq[c] - r[c];
                 }
             }
 #pragma unroll
-            for (int e = 0; e < NC; e++) Cp[e] = c0[e];
+            for (int e = 0; e < NC; e++) {
+                Cp[e] = Cc[e];
+                if (ZC) Cc[e] = Cn[e];
+            }
+            if (ZC) {
+#pragma unroll
+                for (int p = 0; p < 3; p++)
+#pragma unroll
+                    for (int q = 0; q < 5; q++) {
+                        Um[p][q] = Uc[p][q];
+                        Uc[p][q] = Up[p][q];
+                    }
+            }
         }
 #pragma unroll
         for (int c = 0; c < 3; c++) {

@@ -333,11 +333,10 @@ agb_status agb_composite_solve(agb_composite* c, double* const* u, const double*
  * library (AGB_NOALLOC_MAX_BLOCKS pairs of doubles, one per block of the
  * residual kernel, held by every GPU that loads the library until exit), so
  * grids of more than AGB_NOALLOC_MAX_BLOCKS blocks (about 33.5M nodes) return
- * AGB_LIMIT.  The first call on a device looks the array's address up (do it
- * before any stream capture on that device) and caches it; a device reset
- * after that call is not supported.  Calls share the array: calls that
- * overlap on the GPU race and give wrong norms.  Runs on `stream` (NULL: the
- * legacy default stream) and returns after it. */
+ * AGB_LIMIT.  The first call on a device looks the array's address up and
+ * caches it; a device reset after that call is not supported.  Calls share
+ * the array: calls that overlap on the GPU race and give wrong norms.  Runs
+ * on `stream` (NULL: the legacy default stream) and returns after it. */
 #define AGB_NOALLOC_MAX_BLOCKS 131072
 agb_status agb_residual_norms_noalloc(int nx, int ny, int nz, const double dx[3], int sym, const double* C_soa,
                                       const int* bc_type, const double* x, const double* b, double* r,
