@@ -37,6 +37,7 @@ SOLVER_VCYCLE, SOLVER_FGMRES = 0, 1
 BOTTOM_BICGSTAB, BOTTOM_DIRECT, BOTTOM_SMOOTHER = 0, 1, 2
 SMOOTHER_JACOBI, SMOOTHER_GS = 0, 1
 OUTER_FP64, OUTER_DFLOAT = 0, 1
+PRECOND_V, PRECOND_F = 0, 1
 K_FAPPLY_F64, K_JACOBI_F64, K_RESIDUAL_F64, K_FAPPLY_F32, K_JACOBI_F32, K_RESIDUAL_F32, K_RESTRICT, K_PROLONG, \
     K_BOTTOM, K_KRYLOV, K_RESIDUAL_DF = range(11)
 
@@ -68,6 +69,7 @@ class SolverOpts(ctypes.Structure):
         ("max_fmg_iter", ctypes.c_int),
         ("smoother", ctypes.c_int),
         ("outer_residual", ctypes.c_int),
+        ("precond_cycle", ctypes.c_int),
     ]
 
 

@@ -86,6 +86,7 @@ cudaError_t launch_recip(const float* in, float* out, int64_t n, cudaStream_t s)
 // out(double) += scale * in(float)
 cudaError_t launch_add_float(const float* in, double* out, int64_t n, double scale, cudaStream_t s);
 cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStream_t s);
+cudaError_t launch_axpy(float a, const float* x, float* y, int64_t n, cudaStream_t s);
 
 // BC::Operator::Elastic::Constant::Init: boundary values into b
 cudaError_t launch_bc_init(double* b, const LevelGeom<double>& G, const BcTable& bc, const double* bcval_dev,

@@ -653,47 +653,55 @@ agb_status vcycle(agb_elastic* h, std::vector<Lev<T>>& L, int l0 = 0) {
     return AGB_OK;
 }
 
-// One F-cycle on A cor = res of the FP64 fine level, as MLMG::mgFcycle runs
-// it for the iterations below max_fmg_iter: the residual restricted to
-// every level, the bottom solve, then on each finer level the interpolated
-// coarse correction as a start (interpAssign: prolongation into a zeroed
+// One F-cycle on A cor = res of the fine level, as MLMG::mgFcycle runs it
+// for the iterations below max_fmg_iter: the residual restricted to every
+// level, the bottom solve, then on each finer level the interpolated coarse
+// correction as a start (interpAssign: prolongation into a zeroed
 // correction), the residual of that start as the right-hand side of a
-// V-cycle from this level, and the start added back.
-agb_status fcycle64(agb_elastic* h) {
-    std::vector<Lev<double>>& L = h->L64;
+// V-cycle from this level, and the start added back.  The FP64 iteration
+// runs it on L64; FGMRES may run it on its hierarchy as the preconditioner
+// (opts.precond_cycle).  It leaves each level's res/rescor and cor/hold
+// pointers swapped.
+template <typename T>
+agb_status fcycle(agb_elastic* h, std::vector<Lev<T>>& L) {
     const int nl = (int)L.size();
     for (int l = 1; l < nl; l++) {
         {
             ProfScope ps(h, AGB_K_RESTRICT, l == 1);
-            CK(launch_restrict<double>(L[l - 1].res, L[l - 1].G, L[l].res, L[l].G, h->stream));
+            CK(launch_restrict<T>(L[l - 1].res, L[l - 1].G, L[l].res, L[l].G, h->stream));
         }
         h->launches++;
     }
-    TRY(bottom<double>(h, L));
+    TRY(bottom<T>(h, L));
     for (int l = nl - 2; l >= 0; l--) {
-        Lev<double>& v = L[l];
-        Lev<double>& c = L[l + 1];
+        Lev<T>& v = L[l];
+        Lev<T>& c = L[l + 1];
         const int64_t n3 = 3 * v.G.N;
-        if (!v.hold) CK(cudaMalloc(&v.hold, sizeof(double) * n3));
-        CK(cudaMemsetAsync(v.cor, 0, sizeof(double) * n3, h->stream));
+        if (!v.hold) CK(cudaMalloc(&v.hold, sizeof(T) * n3));
+        CK(cudaMemsetAsync(v.cor, 0, sizeof(T) * n3, h->stream));
         {
             ProfScope ps(h, AGB_K_PROLONG, l == 0);
-            CK(launch_prolong_add<double>(c.cor, c.G, v.cor, v.G, h->stream));
+            CK(launch_prolong_add<T>(c.cor, c.G, v.cor, v.G, h->stream));
         }
         {
-            ProfScope ps(h, AGB_K_RESIDUAL_F64, l == 0);
-            CK(launch_residual<double>(h->sym, v.cor, v.res, v.C, v.G, h->bc, v.rescor, nullptr, nullptr, h->stream));
+            ProfScope ps(h, Fam<T>::R, l == 0);
+            if (use_zm<T>(h, v, l))
+                CK(level_zm<T>(h, v, 2, v.cor, v.res, nullptr, T(0), v.rescor));
+            else
+                CK(launch_residual<T>(h->sym, v.cor, v.res, v.C, v.G, h->bc, v.rescor, nullptr, nullptr, h->stream));
         }
         h->launches += 2;
         // res <- res - A start; keep the start; V-cycle; add the start back
         std::swap(v.res, v.rescor);
         std::swap(v.cor, v.hold);
-        TRY(vcycle<double>(h, L, l));
-        CK(launch_axpy(1.0, v.hold, v.cor, n3, h->stream));
+        TRY(vcycle<T>(h, L, l));
+        CK(launch_axpy(T(1), v.hold, v.cor, n3, h->stream));
         h->launches++;
     }
     return AGB_OK;
 }
+
+agb_status fcycle64(agb_elastic* h) { return fcycle<double>(h, h->L64); }
 
 // FP64 residual of level 0 into L64[0].res and its norms (host copy)
 // double-float state of the mixed solve: the fine stiffness as hi + lo
@@ -839,16 +847,30 @@ agb_status fgmres_cycle(agb_elastic* h, std::vector<Lev<T>>& L, const T* r, doub
         // correction in Z_j directly (the smoother ping-pongs cor and tmp, so
         // an odd sweep count leaves it in the other buffer: copied back).
         {
+            const bool fc = h->opts.precond_cycle == AGB_PRECOND_F;
+            if (fc && !top.hold) CK(cudaMalloc(&top.hold, sizeof(T) * n));
             T* res0 = top.res;
             T* cor0 = top.cor;
             T* tmp0 = top.tmp;
-            top.res = K.V[j];
+            T* rescor0 = top.rescor;
+            T* hold0 = top.hold;
+            // the V-cycle only reads its right-hand side, so it reads V_j in
+            // place; the F-cycle's V-cycle from the fine level writes where
+            // the right-hand side was (it swaps res and rescor), so it gets
+            // a copy of V_j
+            if (fc) CK(cudaMemcpyAsync(res0, K.V[j], sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
+            else top.res = K.V[j];
             top.cor = K.Z[j];
-            const agb_status vs = vcycle<T>(h, L);
+            const agb_status vs = fc ? fcycle<T>(h, L) : vcycle<T>(h, L);
             T* out = top.cor;
+            // the F-cycle also swaps cor and hold, so Z_j passes through the
+            // level's work pointers; the level gets its own buffers back (the
+            // result is in one of them or in Z_j)
             top.res = res0;
             top.cor = cor0;
             top.tmp = tmp0;
+            top.rescor = rescor0;
+            top.hold = hold0;
             TRY(vs);
             if (out != K.Z[j]) CK(cudaMemcpyAsync(K.Z[j], out, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
         }
@@ -1167,6 +1189,7 @@ agb_status agb_default_opts(agb_solver_opts* o) {
     o->max_fmg_iter = 100000000;
     o->smoother = AGB_SMOOTHER_JACOBI;
     o->outer_residual = AGB_OUTER_FP64;
+    o->precond_cycle = AGB_PRECOND_V;
     return AGB_OK;
 }
 
@@ -1186,6 +1209,8 @@ static agb_status check_opts(const agb_solver_opts* o) {
         return fail(AGB_BAD_ARG, "unknown smoother");
     if (o->outer_residual != AGB_OUTER_FP64 && o->outer_residual != AGB_OUTER_DFLOAT)
         return fail(AGB_BAD_ARG, "unknown outer_residual");
+    if (o->precond_cycle != AGB_PRECOND_V && o->precond_cycle != AGB_PRECOND_F)
+        return fail(AGB_BAD_ARG, "unknown precond_cycle");
     if (o->solver == AGB_SOLVER_FGMRES && (o->krylov_dim < 1 || o->krylov_dim > 39))
         return fail(AGB_BAD_ARG, "krylov_dim must lie in [1, 39]");
     if (o->solver == AGB_SOLVER_FGMRES && !(o->inner_tol > 0.0 && o->inner_tol < 1.0))

@@ -589,12 +589,17 @@ cudaError_t launch_add_float(const float* in, double* out, int64_t n, double sca
     return cudaGetLastError();
 }
 
-__global__ void k_axpy(double a, const double* __restrict__ x, double* __restrict__ y, int64_t n) {
+template <typename T>
+__global__ void k_axpy(T a, const T* __restrict__ x, T* __restrict__ y, int64_t n) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
         y[q] += a * x[q];
 }
 cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStream_t s) {
-    k_axpy<<<flat_blocks(n), 256, 0, s>>>(a, x, y, n);
+    k_axpy<double><<<flat_blocks(n), 256, 0, s>>>(a, x, y, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_axpy(float a, const float* x, float* y, int64_t n, cudaStream_t s) {
+    k_axpy<float><<<flat_blocks(n), 256, 0, s>>>(a, x, y, n);
     return cudaGetLastError();
 }
 

@@ -57,6 +57,8 @@ def default_opts(**kw):
             v = {"vcycle": L.SOLVER_VCYCLE, "fgmres": L.SOLVER_FGMRES}[v]
         if k == "outer_residual" and isinstance(v, str):
             v = {"fp64": L.OUTER_FP64, "dfloat": L.OUTER_DFLOAT}[v]
+        if k == "precond_cycle" and isinstance(v, str):
+            v = {"v": L.PRECOND_V, "f": L.PRECOND_F}[v]
         if k == "smoother" and isinstance(v, str):
             v = {"jacobi": L.SMOOTHER_JACOBI, "gs": L.SMOOTHER_GS}[v]
         if k == "bottom_solver" and isinstance(v, str):

@@ -91,6 +91,8 @@ def parse():
     p.add_argument("--post", type=int, default=1, help="Fsmooth calls after prolongation in the FP32 V-cycle")
     p.add_argument("--smoother", default="jacobi", choices=["jacobi", "gs"],
                    help="FP32 smoother: damped Jacobi (the reference's) or multicolour Gauss-Seidel")
+    p.add_argument("--precond", default="v", choices=["v", "f"],
+                   help="FGMRES preconditioner: one V-cycle or one F-cycle")
     p.add_argument("--outer", default="dfloat", choices=["fp64", "dfloat"],
                    help="outer residual and update of the mixed solve: FP64 or double-float on the FP32 pipe")
     p.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison solves")
@@ -299,7 +301,7 @@ def reduce_max(x, dist, device):
 
 
 # --------------------------------------------------------------- GPU helpers
-def fast_opts(A, n, args=None, smoother="jacobi", outer="dfloat"):
+def fast_opts(A, n, args=None, smoother="jacobi", outer="dfloat", precond=None):
     """The fast path's options: mixed FGMRES(V(1,1)), direct 5^3 bottom,
     double-float outer residual."""
     pre = args.pre if args else 1
@@ -307,7 +309,7 @@ def fast_opts(A, n, args=None, smoother="jacobi", outer="dfloat"):
     kw = dict(precision=1, solver="fgmres", inner_tol=args.inner_tol if args else 1e-4,
               krylov_dim=args.krylov if args else 20, bottom_solver="direct",
               max_coarsening_level=max(nlevels(n) - 2, 0), pre_smooth=pre, post_smooth=post,
-              outer_residual=outer)
+              outer_residual=outer, precond_cycle=precond or (args.precond if args else "v"))
     if smoother == "gs":
         kw["smoother"] = 1
     return A.default_opts(**kw)
@@ -381,6 +383,9 @@ def compare_fp64(A, torch, n, C, F0, bc, dx, net, name):
            "timing": "host wall clock around one synchronous C-ABI call, device-resident inputs"}
     out["learned_mixed_gs_smoother"] = guarded(
         lambda: rep_summary(*timed_solve(A, torch, n, C, F0, bc, dx, fast_opts(A, n, smoother="gs"), net=net,
+                                         repeats=2)[1:]))
+    out["learned_mixed_fcycle_precond"] = guarded(
+        lambda: rep_summary(*timed_solve(A, torch, n, C, F0, bc, dx, fast_opts(A, n, precond="f"), net=net,
                                          repeats=2)[1:]))
     x64, rep64, sec64 = timed_solve(A, torch, n, C, F0, bc, dx, fp64_fgmres_opts(A, n))
     out["fp64_fgmres_direct_bottom"] = rep_summary(rep64, sec64)
@@ -504,7 +509,7 @@ def main():
     pre, post = (args.pre, args.post) if prec else (2, 2)
     okw = dict(precision=prec, inner_cycles=args.inner, solver=args.solver, inner_tol=args.inner_tol,
                krylov_dim=args.krylov, bottom_solver="direct", max_coarsening_level=max(nlevels(n) - 2, 0),
-               pre_smooth=pre, post_smooth=post)
+               pre_smooth=pre, post_smooth=post, precond_cycle=args.precond)
     if args.smoother == "gs":
         okw["smoother"] = 1
     if prec:
@@ -744,6 +749,7 @@ def main():
         "gpu_solver": {"precision": args.precision, "solver": args.solver, "inner_tol": args.inner_tol,
                        "outer_residual": (args.outer if prec else "fp64"),
                        "krylov_dim": args.krylov, "bottom": "direct 5^3",
+                       "preconditioner": {"v": "one V-cycle", "f": "one F-cycle"}[args.precond],
                        "smoothing": "V(%d,%d), %s" % (pre, post, "2 damped-Jacobi sweeps per Fsmooth call"
                                                       if args.smoother == "jacobi" else
                                                       "multicolour Gauss-Seidel sweeps"),

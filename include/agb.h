@@ -89,6 +89,15 @@ typedef enum { AGB_SMOOTHER_JACOBI = 0, AGB_SMOOTHER_GS = 1 } agb_smoother;
  * the FP64 form). */
 typedef enum { AGB_OUTER_FP64 = 0, AGB_OUTER_DFLOAT = 1 } agb_outer_residual;
 
+/* The FGMRES preconditioner (no counterpart in the reference, whose MLMG has
+ * no Krylov outer iteration): one V-cycle on the correction equation, or one
+ * F-cycle (the reference's mgFcycle form of its FP64 iteration: the residual
+ * restricted to every level, the bottom solve, then on each finer level the
+ * interpolated coarser correction as the start of a V-cycle).  Where the
+ * F-cycle is unstable (a sharp stiffness jump: the reference's F-cycle
+ * iteration stalls there too) FGMRES with it may not converge. */
+typedef enum { AGB_PRECOND_V = 0, AGB_PRECOND_F = 1 } agb_precond_cycle;
+
 /* Solver settings; field names follow the reference's `solver.*` keys
  * (Solver::Nonlocal::Linear::Parse, src/Solver/Nonlocal/Linear.H:296-382). */
 typedef struct agb_solver_opts {
@@ -121,6 +130,7 @@ typedef struct agb_solver_opts {
                                  iteration is an F-cycle (src/Solver/Nonlocal/Linear.H:261) (100000000) */
     int smoother;             /* agb_smoother: the Fsmooth of every level (AGB_SMOOTHER_JACOBI) */
     int outer_residual;       /* agb_outer_residual of the mixed FGMRES solve (AGB_OUTER_FP64) */
+    int precond_cycle;        /* agb_precond_cycle of FGMRES (AGB_PRECOND_V) */
 } agb_solver_opts;
 
 typedef struct agb_solve_report {

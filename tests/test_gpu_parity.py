@@ -349,16 +349,21 @@ def test_mixed_precision_solve(agb, oracle, case):
     assert rel(u, xo) <= 1e-7
 
 
-@pytest.mark.parametrize("prec", [0, 1])
-@pytest.mark.parametrize("case", ["c1-iso", "voronoi-mm"])
-def test_fgmres_solve(agb, oracle, case, prec):
-    """FGMRES preconditioned by one V-cycle (FP64, or FP32 inside FP64
-    refinement) reaches the same solution as the oracle's V-cycle solve."""
+@pytest.mark.parametrize("case,prec,precond", [("c1-iso", 0, "v"), ("c1-iso", 1, "v"), ("voronoi-mm", 0, "v"),
+                                               ("voronoi-mm", 1, "v"), ("voronoi-mm", 0, "f"),
+                                               ("voronoi-mm", 1, "f")])
+def test_fgmres_solve(agb, oracle, case, prec, precond):
+    """FGMRES preconditioned by one V-cycle or one F-cycle (FP64, or FP32
+    inside FP64 refinement) reaches the same solution as the oracle's
+    V-cycle solve.  (On config 1's sharp inclusion the F-cycle is unstable
+    before 1e-10 -- the reference's own F-cycle iteration stalls near 7e-9
+    there -- and FGMRES with it does not reach 1e-10: not a preconditioner
+    for that medium.)"""
     C, F0, bc, dx = CASES[case]()
     u0, b, rhs, bt = newton_problem(agb, oracle, C, F0, bc, dx)
     # against the V-cycle iteration (max_fmg_iter 0), which FGMRES wraps
     xo, rep_o, _ = oracle.solve(C, bt, rhs, dx, tol_rel=1e-10, max_fmg_iter=0)
-    with make_op(agb, C, bc, dx, solver=1, precision=prec, bottom_solver=1,
+    with make_op(agb, C, bc, dx, solver=1, precision=prec, bottom_solver=1, precond_cycle=precond,
                  max_coarsening_level=oracle.num_levels(*C.shape[:3]) - 2) as op:
         u = u0.copy()
         rep = agb.Newton(op).solve(u, b, F0, tol_rel=1e-10, tol_abs=0.0)
