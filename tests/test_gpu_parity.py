@@ -303,20 +303,26 @@ def test_f32_jacobi_and_residual_vs_oracle(agb, oracle, case):
     assert er <= 2e-6
 
 
+@pytest.mark.parametrize("bcase", ["random", "xclamp"])
 @pytest.mark.parametrize("dims", [(41, 19, 37), (3, 3, 3), (35, 9, 4), (66, 11, 97)])
 @pytest.mark.parametrize("sym", ["mm", "iso"])
-def test_zmarch_tma_ragged_grids(agb, oracle, dims, sym):
+def test_zmarch_tma_ragged_grids(agb, oracle, dims, sym, bcase):
     """TMA-staged FP32 Fapply on grids whose interior does not fill the
     32 x 8 tiles or the z chunks (partial tiles, a 1-node interior, a pitch
     that needs padding) against the oracle's FP64 operator, to FP32
-    rounding; random boundary types exercise the separate face kernel.  The
-    isotropic kernel stages two planes ahead, the major-minor one one."""
+    rounding; random boundary types and the clamped faces of the tension
+    test exercise the separate face kernel.  The isotropic kernel stages two
+    planes ahead, the major-minor one one."""
     nx, ny, nz = dims
     if sym == "mm":
         C = np.ascontiguousarray(agb.synth.voronoi_cubic(max(dims), 16, seed=5)[0][:nz, :ny, :nx])
     else:
         C = np.ascontiguousarray(np.random.default_rng(5).uniform(1.0, 10.0, (nz, ny, nx, 2)))
-    bc = P.random_bc(77)
+    if bcase == "random":
+        bc = P.random_bc(77)
+    else:
+        from alamo_gb300 import bc as B
+        bc = B.TensionTest("uniaxial_stress_clamp", disp=0.01)
     dx = np.array([1 / (nx - 1), 1 / (ny - 1), 1 / (nz - 1)])
     u = P.random_field((3, nz, ny, nx), 78)
     bt, _ = bc.tables()
