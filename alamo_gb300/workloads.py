@@ -18,6 +18,9 @@ Workloads (unit cube, node coordinates i*dx):
                    src/Set/Matrix4_MajorMinor.H:518-547)
   spheres_diffuse  non-overlapping spheres with the diffuse profile of the
                    reference's ellipse initial condition (src/IC/Ellipse.H:56-75)
+
+and, at the end, the known-answer problems of the reference's Eshelby,
+PlateHole and neo-Hookean tests.
 """
 import math
 
@@ -251,3 +254,156 @@ def spheres_diffuse(n, nspheres=200, seed=3, rmin=0.02, rmax=0.06, eps=None, con
     C[..., 0] = (1.0 - e) * 1.0 + e * contrast
     C[..., 1] = (1.0 - e) * 1.0 + e * contrast
     return C, f0, dx, len(sp)
+
+
+# ------------------------------------------------------------------
+# Known-answer problems of the reference's regression tests, restated on
+# this library's grids; the tests and the benchmark's measurements of the
+# psi, nonlinear and AMR paths use them.
+
+def _trapz(x, y):
+    return float(np.sum(0.5 * (y[1:] + y[:-1]) * (x[1:] - x[:-1])))
+
+
+# tests/Eshelby/input
+ESHELBY_E, ESHELBY_NU = 210.0, 0.3
+ESHELBY_AXES = (1.0, 0.75, 0.5)
+ESHELBY_EPS = 0.1
+ESHELBY_EIGEN = 0.001
+
+
+def eshelby_fields(xs, ys=None, zs=None):
+    """Stiffness (lambda, mu per node) and dilatational eigenstrain of the
+    reference's Eshelby inclusion (see eshelby) at the nodes xs x ys x zs
+    (ys, zs default to xs)."""
+    from scipy.special import erf
+    ys = xs if ys is None else ys
+    zs = xs if zs is None else zs
+    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+    a = ESHELBY_AXES
+    q = (X / a[0]) ** 2 + (Y / a[1]) ** 2 + (Z / a[2]) ** 2
+    norm = np.sqrt((X / a[0] ** 2) ** 2 + (Y / a[1] ** 2) ** 2 + (Z / a[2] ** 2) ** 2)
+    del X, Y, Z
+    with np.errstate(divide="ignore", invalid="ignore"):
+        eta = 0.5 - 0.5 * erf((q - 1.0) / ESHELBY_EPS / norm)
+    eta[norm == 0.0] = 1.0
+    E, nu = ESHELBY_E, ESHELBY_NU
+    C = np.empty(eta.shape + (2,))
+    C[..., 0] = E * nu / (1 + nu) / (1 - 2 * nu)
+    C[..., 1] = E / 2 / (1 + nu)
+    return C, ESHELBY_EIGEN * eta
+
+
+
+def eshelby_amr_levels(nvs=(63, 63, 95)):
+    """tests/Eshelby with four levels on [-8, 8]^3: level 0 65^3 (spacing
+    1/4) and boxes about the origin of nvs valid nodes at spacings 1/8, 1/16
+    and 1/32, each lo even (the composite solve's rule), their arrays
+    covering the box plus one ghost ring.  The finest box's faces lie outside
+    the inclusion's diffuse boundary.  Returns (n0, dx0, boxes, Cs, F0s, hw);
+    the boundary condition is zero displacement (bc.Constant())."""
+    n0, hw = 65, 8.0
+    dx0 = 2 * hw / (n0 - 1)
+    xs = -hw + dx0 * np.arange(n0)
+    C0, F00 = eshelby_fields(xs)
+    Cs, F0s, boxes = [C0], [F00], []
+    for l, nv in enumerate(nvs, start=1):
+        h = dx0 / 2 ** l
+        lo = int(round((hw - h * (nv - 1) / 2) / h))
+        lo -= lo % 2
+        c = -hw + h * (lo - 1 + np.arange(nv + 2))
+        C, F0 = eshelby_fields(c)
+        Cs.append(C)
+        F0s.append(F0)
+        boxes.append((lo, nv))
+    return n0, dx0, boxes, Cs, F0s, hw
+
+
+# tests/PlateHole/input: [-16, 16]^2, a circular void of radius 1 (psi from
+# the inverted ellipse IC, eps 0.2), E = 1, nu = 0.3 in plane stress,
+# TensionTest uniaxial_stress with disp 0.01, elasticop.small 1e-16
+PLATEHOLE_HALF = 16.0
+PLATEHOLE_EPS = 0.2
+PLATEHOLE_SMALL = 1e-16
+# far-field stress of tests/PlateHole/test (the value its Kirsch curves use)
+PLATEHOLE_SIG0 = 0.0003075
+
+
+def platehole(nxy, nz):
+    """The reference's 2D plane-stress PlateHole test restated in 3D: a plate
+    of nxy^2 x nz nodes over [-16, 16]^2 (cubic cells) whose solution does not
+    depend on z.  The z faces are displacement rows for u_z (= 0) and
+    traction rows for u_x, u_y (sigma_xz = sigma_yz = 0, i.e. du/dz = 0
+    one-sided), so every z-plane carries the 2D plane-strain problem; the
+    plane-stress Lame constant lambda 2 mu / (lambda + 2 mu)
+    (src/Model/Solid/Linear/Isotropic.H:183-184) then makes it the
+    reference's plane-stress problem.  psi is the cell field of
+    src/IC/Ellipse.H:58-61 with invert: 1/2 + 1/2 erf((r^2 - 1) / eps / r) at
+    cell centres, r the distance from the z axis.  Returns (C, psi, bc, dx)."""
+    from scipy.special import erf
+    from . import bc as B
+    hw = PLATEHOLE_HALF
+    dx = 2 * hw / (nxy - 1)
+    E, nu = 1.0, 0.3
+    lam = E * nu / (1 + nu) / (1 - 2 * nu)
+    mu = E / 2 / (1 + nu)
+    C = np.empty((nz, nxy, nxy, 2))
+    C[..., 0] = lam * (1.0 - lam / (2 * mu + lam))
+    C[..., 1] = mu
+    xc = -hw + dx * (np.arange(nxy - 1) + 0.5)
+    Y, X = np.meshgrid(xc, xc, indexing="ij")
+    r = np.sqrt(X ** 2 + Y ** 2)
+    psi2 = 0.5 + 0.5 * erf((r ** 2 - 1.0) / PLATEHOLE_EPS / r)
+    psi = np.ascontiguousarray(np.broadcast_to(psi2, (nz - 1,) + psi2.shape))
+    bc = B.TensionTest("uniaxial_stress", disp=0.01)
+    for f in B.FACES:
+        if "zlo" in f or "zhi" in f:
+            bc.set(f, 2, "displacement", 0.0)
+    return C, psi, bc, dx
+
+
+def kirsch(x, y, a=1.0, s0=PLATEHOLE_SIG0):
+    """Kirsch's stresses about a circular hole of radius a in an infinite
+    plate under uniaxial tension s0 along x (polar components, rotated to
+    xx, yy, xy)."""
+    r = np.sqrt(x ** 2 + y ** 2)
+    t = np.arctan2(y, x)
+    q2, q4 = (a / r) ** 2, (a / r) ** 4
+    c2, s2 = np.cos(2 * t), np.sin(2 * t)
+    srr = 0.5 * s0 * (1 - q2) + 0.5 * s0 * (1 - 4 * q2 + 3 * q4) * c2
+    stt = 0.5 * s0 * (1 + q2) - 0.5 * s0 * (1 + 3 * q4) * c2
+    srt = -0.5 * s0 * (1 + 2 * q2 - 3 * q4) * s2
+    c, s = np.cos(t), np.sin(t)
+    sxx = srr * c * c - 2 * srt * c * s + stt * s * s
+    syy = srr * s * s + 2 * srt * c * s + stt * c * c
+    sxy = (srr - stt) * s * c + (c * c - s * s) * srt
+    return sxx, syy, sxy
+
+
+def platehole_errors(xs, sxx, syy, sxy, y=2.0):
+    """tests/PlateHole/test: along the ray at height y over x in [-16, 16],
+    the L2 distance of each stress component from Kirsch's (1000 points,
+    the numerical curve interpolated onto them) over |integral of the
+    numerical sigma_xx|; the test's tolerance is 0.01."""
+    xr = np.linspace(-PLATEHOLE_HALF, PLATEHOLE_HALF, 1000)
+    ref = kirsch(xr, np.full_like(xr, y))
+    norm = abs(_trapz(xs, sxx))
+    return np.array([np.sqrt(_trapz(xr, (np.interp(xr, xs, s) - r) ** 2)) / norm
+                     for s, r in zip((sxx, syy, sxy), ref)])
+
+
+def neohookean_twophase(n, seed=5, disp=0.02):
+    """A two-phase NeoHookean cube on the unit cube: (mu, kappa) per node,
+    mu 3 (kappa 9) in a central sphere of radius 0.3 and 1 (3) outside, mu
+    perturbed by 5 % uniform noise; x faces clamped, the x+ face pulled by
+    u_x = disp, the other faces traction-free (TensionTest
+    uniaxial_stress_clamp).  Returns (model, bc, dx)."""
+    from . import bc as B
+    rng = np.random.default_rng(seed)
+    x = np.arange(n) / (n - 1)
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    inc = ((X - 0.5) ** 2 + (Y - 0.5) ** 2 + (Z - 0.5) ** 2) < 0.3 ** 2
+    model = np.empty((n, n, n, 2))
+    model[..., 0] = np.where(inc, 3.0, 1.0) * (1 + 0.05 * rng.uniform(-1, 1, (n, n, n)))
+    model[..., 1] = np.where(inc, 9.0, 3.0)
+    return model, B.TensionTest("uniaxial_stress_clamp", disp=disp), 1.0 / (n - 1)

@@ -403,6 +403,155 @@ def compare_fp64(A, torch, n, C, F0, bc, dx, net, name):
     return out
 
 
+def next_rows(A, torch, O, c2):
+    """The rows beyond the benchmark step, each timed on the GPU (host wall
+    clock around synchronous C-ABI calls) and by the oracle on all host
+    threads, with the GPU result's distance from the oracle's: stress,
+    strain and energy (Elastic::Stress/Strain/Energy) at 257^3, the psi
+    void terms on the PlateHole plate (with its Kirsch errors), the Newton
+    loop of a NeoHookean medium at 65^3, and the four-level AMR composite
+    solve of the Eshelby inclusion."""
+    import ctypes
+    from alamo_gb300 import _lib as L
+    from alamo_gb300 import bc as B
+    from alamo_gb300 import workloads as W
+    out = {}
+
+    def stress():
+        name, n, C, bc, dx = c2
+        N = n ** 3
+        u = np.random.default_rng(7).uniform(-1e-3, 1e-3, (3, n, n, n))
+        dev = torch.device("cuda", torch.cuda.current_device())
+        u_d = torch.from_numpy(u).to(dev)
+        s_d = torch.empty(9 * N, dtype=torch.float64, device=dev)
+        e_d = torch.empty(9 * N, dtype=torch.float64, device=dev)
+        w_d = torch.empty(N, dtype=torch.float64, device=dev)
+        with A.Elastic(n, dx, "majorminor") as op:
+            op.SetModel(np.ascontiguousarray(C))
+            op.SetBC(bc)
+
+            def call():
+                L.check(L.lib().agb_elastic_stress_strain(
+                    op.h, ctypes.c_void_p(u_d.data_ptr()), None, 0, ctypes.c_void_p(s_d.data_ptr()),
+                    ctypes.c_void_p(e_d.data_ptr()), ctypes.c_void_p(w_d.data_ptr()), L.MEM_DEVICE))
+            call()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(5):
+                call()
+            torch.cuda.synchronize()
+            sec = (time.perf_counter() - t0) / 5
+        nbytes = N * (24 + 8 * C.shape[-1] + 72 + 72 + 8)
+        d = {"workload": name + "; u uniform in [-1e-3, 1e-3]", "seconds": sec,
+             "bytes_per_node": nbytes // N, "achieved_gbs": nbytes / sec / 1e9}
+        if O:
+            t0 = time.perf_counter()
+            so, eo, wo = O.stress_strain(C, None, u, dx)
+            d["oracle_seconds"] = time.perf_counter() - t0
+            d["stress_vs_oracle"] = rel_err(s_d.view(n, n, n, 9).cpu().numpy(), so.reshape(n, n, n, 9))
+            d["strain_vs_oracle"] = rel_err(e_d.view(n, n, n, 9).cpu().numpy(), eo.reshape(n, n, n, 9))
+        return d
+    out["stress_strain"] = guarded(stress)
+
+    def psi():
+        nxy, nz = 129, 17
+        C, pc, bc, dx = W.platehole(nxy, nz)
+        opts = A.default_opts(precision="fp64", solver="vcycle", bottom_solver="smoother", max_iter=400)
+        with A.Elastic((nxy, nxy, nz), dx, "isotropic", opts) as op:
+            op.SetModel(np.ascontiguousarray(C))
+            op.SetBC(bc)
+            op.SetPsi(pc, W.PLATEHOLE_SMALL)
+            b = op.bc_init()
+            u = np.zeros((3, nz, nxy, nxy))
+            t0 = time.perf_counter()
+            rep = A.Newton(op).solve(u, b, None, tol_rel=1e-10, tol_abs=1e-16)
+            sec = time.perf_counter() - t0
+            sg = op.stress_strain(u)[0]
+        j = int(round((2.0 + W.PLATEHOLE_HALF) / dx))
+        row = sg[nz // 2, j]
+        xs = -W.PLATEHOLE_HALF + dx * np.arange(nxy)
+        err = W.platehole_errors(xs, row[:, 0, 0], row[:, 1, 1], row[:, 0, 1])
+        d = {"workload": "PlateHole restated as a z-invariant %d^2 x %d plate, psi void of radius 1" % (nxy, nz),
+             "gpu": rep_summary(rep, sec), "kirsch_errors_xx_yy_xy": [float(e) for e in err],
+             "kirsch_tolerance": 0.01}
+        if O:
+            bt, bv = bc.tables()
+            O.set_psi(pc, W.PLATEHOLE_SMALL)
+            try:
+                t0 = time.perf_counter()
+                zero = np.zeros_like(u)
+                rhs = O.build_rhs(C, None, bt, zero, O.bc_init(np.zeros_like(u), bt, bv), dx)
+                xo, rep_o, _ = O.solve(C, bt, rhs, dx, tol_rel=1e-10, tol_abs=1e-16,
+                                       opts=O.default_opts(bottom_solver=2, max_iter=400))
+                d["oracle_seconds"] = time.perf_counter() - t0
+                d["oracle_cycles"] = rep_o.iters
+            finally:
+                O.set_psi(None)
+            d["gpu_vs_oracle"] = rel_err(u, xo)
+        return d
+    out["psi_platehole"] = guarded(psi)
+
+    def newton():
+        n, nri = 65, 4
+        model, bc, dx = W.neohookean_twophase(n)
+        mcl = max(nlevels(n) - 2, 0)
+        opts = A.default_opts(precision="mixed", solver="fgmres", bottom_solver="direct", max_coarsening_level=mcl)
+        with A.Elastic(n, dx, "major", opts) as op:
+            op.SetBC(bc)
+            b = op.bc_init()
+            u = np.zeros((3, n, n, n))
+            t0 = time.perf_counter()
+            rep = A.Newton(op, nriters=nri).solve_neohookean(np.ascontiguousarray(model), u, b, tol_rel=1e-10)
+            sec = time.perf_counter() - t0
+        d = {"workload": "two-phase NeoHookean cube %d^3, clamped x faces, u_x = 0.02, %d Newton iterations"
+                         % (n, nri), "gpu_seconds": sec, "last_increment": rep["relnorm"]}
+        if O:
+            bt, bv = bc.tables()
+            t0 = time.perf_counter()
+            x = np.zeros((3, n, n, n))
+            b0 = O.bc_init(x, bt, bv)
+            for _ in range(nri):
+                dw, ddw = O.neohookean_field(model, x, dx)
+                rhs = O.rhs_dw(dw, bt, x, b0, dx)
+                du, rep_o, _ = O.solve(np.ascontiguousarray(ddw), bt, rhs, dx, tol_rel=1e-10, max_iter=200,
+                                       bottom_solver=1, max_coarsening_level=mcl)
+                x = x + du
+            d["oracle_seconds"] = time.perf_counter() - t0
+            d["gpu_vs_oracle"] = rel_err(u, x)
+        return d
+    out["newton_neohookean"] = guarded(newton)
+
+    def amr():
+        from alamo_gb300.composite import Composite
+        n0, dx0, boxes, Cs, F0s, hw = W.eshelby_amr_levels()
+        mcl = nlevels(n0) - 2
+        opts = A.default_opts(precision=0, bottom_solver="direct", max_coarsening_level=mcl, max_iter=80)
+        with Composite(n0, dx0, boxes, "isotropic", opts) as c:
+            c.SetBC(B.Constant())
+            for l, C in enumerate(Cs):
+                c.SetModel(l, C)
+            t0 = time.perf_counter()
+            ug, itg, rn = c.solve(F0=F0s, tol_rel=1e-7)
+            sec = time.perf_counter() - t0
+        d = {"workload": "Eshelby inclusion, 4 levels: 65^3 and boxes of 63^3, 63^3, 95^3 valid nodes",
+             "gpu_seconds": sec, "iterations": itg, "final_rel_resnorm": rn}
+        if O:
+            import composite as CP
+            bt, bv = B.Constant().tables()
+            levels = [CP.Level((n0,) * 3, dx0, None, (n0,) * 3, Cs[0], bt, bv)]
+            for l, (lo, nv) in enumerate(boxes, start=1):
+                levels.append(CP.Level((nv + 2,) * 3, dx0 / 2 ** l, (lo,) * 3, (nv,) * 3, Cs[l], bt, bv))
+            oo = O.default_opts(max_fmg_iter=0, bottom_solver=1, max_coarsening_level=mcl)
+            t0 = time.perf_counter()
+            uo, ito, _ = CP.Composite(levels, F0s=F0s, opts0=oo, optsf=oo).solve(tol_rel=1e-7, max_iter=80)
+            d["oracle_seconds"] = time.perf_counter() - t0
+            d["oracle_iterations"] = ito
+            d["gpu_vs_oracle_max_over_levels"] = max(rel_err(a, b_)["rel_inf"] for a, b_ in zip(ug, uo))
+        return d
+    out["amr_composite"] = guarded(amr)
+    return out
+
+
 def extra_configs(A, torch, net, O, args):
     """Configs 1, 3, 4 and 5, each in minutes at most."""
     from alamo_gb300 import bc as B
@@ -736,8 +885,10 @@ def main():
     op.close()
     del C_dev, F0_dev, u_dev, b_dev
     torch.cuda.empty_cache()
+    nextr = None
     if rank == 0 and not args.no_extra and args.config == "c2" and not args.n:
         extra = guarded(lambda: extra_configs(A, torch, net, O, args))
+        nextr = guarded(lambda: next_rows(A, torch, O, (name, n, C, bc, dx)))
 
     rep = reports[-1] if reports else {}
     line = {
@@ -766,7 +917,7 @@ def main():
         "plain_fp64": plain, "fp64_fgmres": fp64_fgmres, "fast_path_fp64_outer_residual": fp64_outer,
         "fast_path_gs_smoother": gs_arm,
         "speedup_vs_plain_fp64": (plain["seconds"] / sec) if plain and "seconds" in plain else None,
-        "fapply": fap, "kernels_in_timed_region": kernels, "other_configs": extra,
+        "fapply": fap, "kernels_in_timed_region": kernels, "other_configs": extra, "next_rows": nextr,
     }
     if rank == 0:
         print(json.dumps(line))

@@ -57,32 +57,9 @@ def iso_as_mm(C):
 
 
 # ------------------------------------------------------------------ Eshelby
-ESHELBY_E, ESHELBY_NU = 210.0, 0.3
-ESHELBY_AXES = (1.0, 0.75, 0.5)
-ESHELBY_EPS = 0.1
-ESHELBY_EIGEN = 0.001
-
-
-def eshelby_fields(xs, ys=None, zs=None):
-    """Stiffness (lambda, mu per node) and dilatational eigenstrain of the
-    reference's Eshelby inclusion (see eshelby) at the nodes xs x ys x zs
-    (ys, zs default to xs)."""
-    from scipy.special import erf
-    ys = xs if ys is None else ys
-    zs = xs if zs is None else zs
-    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
-    a = ESHELBY_AXES
-    q = (X / a[0]) ** 2 + (Y / a[1]) ** 2 + (Z / a[2]) ** 2
-    norm = np.sqrt((X / a[0] ** 2) ** 2 + (Y / a[1] ** 2) ** 2 + (Z / a[2] ** 2) ** 2)
-    del X, Y, Z
-    with np.errstate(divide="ignore", invalid="ignore"):
-        eta = 0.5 - 0.5 * erf((q - 1.0) / ESHELBY_EPS / norm)
-    eta[norm == 0.0] = 1.0
-    E, nu = ESHELBY_E, ESHELBY_NU
-    C = np.empty(eta.shape + (2,))
-    C[..., 0] = E * nu / (1 + nu) / (1 - 2 * nu)
-    C[..., 1] = E / 2 / (1 + nu)
-    return C, ESHELBY_EIGEN * eta
+from alamo_gb300.workloads import (ESHELBY_AXES, ESHELBY_E, ESHELBY_EIGEN, ESHELBY_EPS, ESHELBY_NU,  # noqa: E402,F401
+                                   PLATEHOLE_EPS, PLATEHOLE_HALF, PLATEHOLE_SIG0, PLATEHOLE_SMALL, eshelby_fields,
+                                   kirsch, platehole, platehole_errors)
 
 
 def eshelby(n, half_width):
@@ -153,74 +130,3 @@ def eshelby_errors(golden, u, sig_normal, half_width, dx):
         serr.append(_integrate(z, np.abs(d)) / _integrate(ref[0], np.abs(exact)))
     return np.array(uerr), np.array(serr)
 
-
-# tests/PlateHole/input: [-16, 16]^2, a circular void of radius 1 (psi from
-# the inverted ellipse IC, eps 0.2), E = 1, nu = 0.3 in plane stress,
-# TensionTest uniaxial_stress with disp 0.01, elasticop.small 1e-16
-PLATEHOLE_HALF = 16.0
-PLATEHOLE_EPS = 0.2
-PLATEHOLE_SMALL = 1e-16
-# far-field stress of tests/PlateHole/test (the value its Kirsch curves use)
-PLATEHOLE_SIG0 = 0.0003075
-
-
-def platehole(nxy, nz):
-    """The reference's 2D plane-stress PlateHole test restated in 3D: a plate
-    of nxy^2 x nz nodes over [-16, 16]^2 (cubic cells) whose solution does not
-    depend on z.  The z faces are displacement rows for u_z (= 0) and
-    traction rows for u_x, u_y (sigma_xz = sigma_yz = 0, i.e. du/dz = 0
-    one-sided), so every z-plane carries the 2D plane-strain problem; the
-    plane-stress Lame constant lambda 2 mu / (lambda + 2 mu)
-    (src/Model/Solid/Linear/Isotropic.H:183-184) then makes it the
-    reference's plane-stress problem.  psi is the cell field of
-    src/IC/Ellipse.H:58-61 with invert: 1/2 + 1/2 erf((r^2 - 1) / eps / r) at
-    cell centres, r the distance from the z axis.  Returns (C, psi, bc, dx)."""
-    from scipy.special import erf
-    hw = PLATEHOLE_HALF
-    dx = 2 * hw / (nxy - 1)
-    E, nu = 1.0, 0.3
-    lam = E * nu / (1 + nu) / (1 - 2 * nu)
-    mu = E / 2 / (1 + nu)
-    C = np.empty((nz, nxy, nxy, 2))
-    C[..., 0] = lam * (1.0 - lam / (2 * mu + lam))
-    C[..., 1] = mu
-    xc = -hw + dx * (np.arange(nxy - 1) + 0.5)
-    Y, X = np.meshgrid(xc, xc, indexing="ij")
-    r = np.sqrt(X ** 2 + Y ** 2)
-    psi2 = 0.5 + 0.5 * erf((r ** 2 - 1.0) / PLATEHOLE_EPS / r)
-    psi = np.ascontiguousarray(np.broadcast_to(psi2, (nz - 1,) + psi2.shape))
-    bc = B.TensionTest("uniaxial_stress", disp=0.01)
-    for f in B.FACES:
-        if "zlo" in f or "zhi" in f:
-            bc.set(f, 2, "displacement", 0.0)
-    return C, psi, bc, dx
-
-
-def kirsch(x, y, a=1.0, s0=PLATEHOLE_SIG0):
-    """Kirsch's stresses about a circular hole of radius a in an infinite
-    plate under uniaxial tension s0 along x (polar components, rotated to
-    xx, yy, xy)."""
-    r = np.sqrt(x ** 2 + y ** 2)
-    t = np.arctan2(y, x)
-    q2, q4 = (a / r) ** 2, (a / r) ** 4
-    c2, s2 = np.cos(2 * t), np.sin(2 * t)
-    srr = 0.5 * s0 * (1 - q2) + 0.5 * s0 * (1 - 4 * q2 + 3 * q4) * c2
-    stt = 0.5 * s0 * (1 + q2) - 0.5 * s0 * (1 + 3 * q4) * c2
-    srt = -0.5 * s0 * (1 + 2 * q2 - 3 * q4) * s2
-    c, s = np.cos(t), np.sin(t)
-    sxx = srr * c * c - 2 * srt * c * s + stt * s * s
-    syy = srr * s * s + 2 * srt * c * s + stt * c * c
-    sxy = (srr - stt) * s * c + (c * c - s * s) * srt
-    return sxx, syy, sxy
-
-
-def platehole_errors(xs, sxx, syy, sxy, y=2.0):
-    """tests/PlateHole/test: along the ray at height y over x in [-16, 16],
-    the L2 distance of each stress component from Kirsch's (1000 points,
-    the numerical curve interpolated onto them) over |integral of the
-    numerical sigma_xx|; the test's tolerance is 0.01."""
-    xr = np.linspace(-PLATEHOLE_HALF, PLATEHOLE_HALF, 1000)
-    ref = kirsch(xr, np.full_like(xr, y))
-    norm = abs(_integrate(xs, sxx))
-    return np.array([np.sqrt(_integrate(xr, (np.interp(xr, xs, s) - r) ** 2)) / norm
-                     for s, r in zip((sxx, syy, sxy), ref)])

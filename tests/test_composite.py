@@ -50,24 +50,13 @@ def uniaxial_levels():
 def eshelby_levels(nvs=(63, 63, 95)):
     """tests/Eshelby on [-8, 8]^3 with four levels: level 0 65^3 (spacing
     1/4) and boxes about the origin of 63 valid nodes from -4 (spacing 1/8),
-    63 from -2 (1/16) and 95 from -1.5 (1/32).  The finest box's faces lie
-    outside the inclusion's diffuse boundary (semi-axes 1, 0.75, 0.5, width
-    0.1), as the reference's gradient tagging keeps them."""
-    n0, hw = 65, 8.0
-    dx0 = 2 * hw / (n0 - 1)
-    xs = -hw + dx0 * np.arange(n0)
-    C0, F00 = P.eshelby_fields(xs)
-    Cs, F0s, boxes = [C0], [F00], []
-    for l, nv in enumerate(nvs, start=1):
-        h = dx0 / 2 ** l
-        lo = int(round((hw - h * (nv - 1) / 2) / h))
-        lo -= lo % 2
-        c = -hw + h * (lo - 1 + np.arange(nv + 2))
-        C, F0 = P.eshelby_fields(c)
-        Cs.append(C)
-        F0s.append(F0)
-        boxes.append((lo, nv))
+    63 from -2 (1/16) and 95 from -1.5 (1/32) (workloads.eshelby_amr_levels).
+    The finest box's faces lie outside the inclusion's diffuse boundary
+    (semi-axes 1, 0.75, 0.5, width 0.1), as the reference's gradient tagging
+    keeps them."""
     from alamo_gb300 import bc as B
+    from alamo_gb300.workloads import eshelby_amr_levels
+    n0, dx0, boxes, Cs, F0s, hw = eshelby_amr_levels(nvs)
     return n0, dx0, boxes, Cs, F0s, B.Constant(), hw
 
 

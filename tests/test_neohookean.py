@@ -159,15 +159,10 @@ def test_major_operator_equals_major_minor_on_minor_symmetric_tensor(oracle):
 
 def neo_problem(n, seed=5, disp=0.02):
     """A two-phase NeoHookean cube (mu, kappa per node), x faces clamped, x+
-    face pulled by u_x = disp, other faces traction-free."""
-    rng = np.random.default_rng(seed)
-    x = np.arange(n) / (n - 1)
-    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
-    inc = ((X - 0.5) ** 2 + (Y - 0.5) ** 2 + (Z - 0.5) ** 2) < 0.3 ** 2
-    model = np.empty((n, n, n, 2))
-    model[..., 0] = np.where(inc, 3.0, 1.0) * (1 + 0.05 * rng.uniform(-1, 1, (n, n, n)))
-    model[..., 1] = np.where(inc, 9.0, 3.0)
-    return model, B.TensionTest("uniaxial_stress_clamp", disp=disp), 1.0 / (n - 1)
+    face pulled by u_x = disp, other faces traction-free
+    (workloads.neohookean_twophase)."""
+    from alamo_gb300.workloads import neohookean_twophase
+    return neohookean_twophase(n, seed, disp)
 
 
 def oracle_newton(oracle, model, bc, dx, nriters, tol=1e-10):
