@@ -40,6 +40,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 #include "agb_launch.h"
 #include "operator.cuh"
 #include "zmarch_tma.h"
@@ -487,14 +489,27 @@ __global__ void k_pad_planes(const float* __restrict__ src, float* __restrict__ 
     }
 }
 
-// planes per block: enough blocks for about two waves of two blocks per SM,
-// at least 4 planes (each block stages 3 extra planes), at most 32
-int zt_kchunk(int ni, int nj, int nk) {
+// planes per block (the z-chunk): the chunk that minimises
+//   ceil(W) / W * (kc + 2) / kc,   W = blocks / (152 * blocks per SM),
+// the idle share of a last, partial wave of blocks times the two extra
+// planes every chunk stages; chunks of 4 to 64 planes.  (257^3 major-minor:
+// 37 planes, 7 chunks, 5.9 waves; 129^3: 15 planes, 9 chunks, 1.9 waves.)
+int zt_kchunk(int ni, int nj, int nk, int per_sm) {
     const int64_t tiles = (int64_t)((ni + TX - 1) / TX) * ((nj + TY - 1) / TY);
-    int64_t kc = tiles * nk / (4 * 152);
-    if (kc < 4) kc = 4;
-    if (kc > 32) kc = 32;
-    return (int)kc;
+    const double slots = 152.0 * per_sm;
+    int best = 4;
+    double best_cost = 1e300;
+    for (int kc = 4; kc <= 64; kc++) {
+        const int chunks = (nk + kc - 1) / kc;
+        if (kc > 4 && (nk + kc - 2) / (kc - 1) == chunks) continue;  // same chunks, more planes each
+        const double w = (double)(tiles * chunks) / slots;
+        const double cost = std::ceil(w) / w * (kc + 2.0) / kc;
+        if (cost < best_cost - 1e-12) {
+            best_cost = cost;
+            best = kc;
+        }
+    }
+    return best;
 }
 
 }  // namespace
@@ -556,7 +571,7 @@ static cudaError_t zt_launch(const CUtensorMap& map, const float* x, const float
         if (dev >= 0 && dev < 64) configured[dev] = true;
     }
     const int ni = G.nx - 2, nj = G.ny - 2, nk = G.nz - 2;
-    const int kc = zt_kchunk(ni, nj, nk);
+    const int kc = zt_kchunk(ni, nj, nk, NC <= 2 ? 3 : 2);
     dim3 blk(TX, TY, 1), grd((ni + TX - 1) / TX, (nj + TY - 1) / TY, (nk + kc - 1) / kc);
     const int fa = G.nx > G.ny ? G.nx : G.ny, fb = G.ny > G.nz ? G.ny : G.nz;
     dim3 fgrd((fa + TX - 1) / TX, (fb + TY - 1) / TY, 6);
